@@ -1,0 +1,167 @@
+// Spatial ADRT levels in the reference's layout (adrtcore.py:29-137). Level m maps data on E^n_{m-1}
+// (stored (N + 2^(m-1) - 1) x N, row = h + 2^(m-1) - 1) to E^n_m ((N + 2^m - 1) x N):
+//   g(h, l*2w + 2t + b) = f(h, l*2w + t) [h >= -t] + f(h + t + b, l*2w + w + t) [h + t + b in [-t, N)],  w = 2^(m-1).
+// Forward: one pass per level over all images and quadrants, the quadrant permutation T_q folded into level 1.
+// Adjoint: the scatter-add of S_m^T is evaluated as a gather (two terms per output), and the last level also applies
+// T_q^T and sums the four quadrants. Additions only, so integer dtypes are exact.
+#include "common.cuh"
+#include "launch.h"
+
+namespace adrt {
+
+static int grid_of(size_t total) {
+    size_t g = (total + 255) / 256;
+    if (g > 65535u * 16) g = 65535u * 16;
+    return (int)(g ? g : 1);
+}
+
+// (T_q x)(i, j) (adrtcore.py:29-39)
+template <typename T> __device__ __forceinline__ T tq_read(const T* x, int N, int q, int i, int j) {
+    switch (q) {
+        case 0: return x[(size_t)j * N + (N - 1 - i)];
+        case 1: return x[(size_t)(N - 1 - i) * N + j];
+        case 2: return x[(size_t)i * N + j];
+        default: return x[(size_t)(N - 1 - j) * N + (N - 1 - i)];
+    }
+}
+
+// one forward level for every (image, quadrant); level 1 reads T_q x, later levels read src; slot stride S elements
+template <typename T>
+__global__ void adrt_fwd_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S) {
+    const int N = 1 << n, w = 1 << (m - 1);
+    const int Hout = N + 2 * w - 1;
+    const size_t per = (size_t)Hout * N;
+    const size_t total = per * 4 * nimg;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t slot = e / per;
+        const size_t rem = e - slot * per;
+        const int row = (int)(rem >> n), s = (int)(rem & (N - 1));
+        const int h = row - (2 * w - 1);
+        const int l = s / (2 * w), rr = s - l * 2 * w, t = rr >> 1, b = rr & 1;
+        const int c0 = l * 2 * w + t, c1 = c0 + w;
+        T acc = 0;
+        if (m == 1) {
+            const int q = (int)(slot & 3);
+            const T* x = src + (slot >> 2) * (size_t)N * N;
+            if (h >= 0 && h < N) acc += tq_read(x, N, q, h, c0);
+            const int h1 = h + b;
+            if (h1 >= 0 && h1 < N) acc += tq_read(x, N, q, h1, c1);
+        } else {
+            const T* f = src + slot * S;
+            const int off = w - 1;
+            if (h >= -t && h < N) acc += f[(size_t)(h + off) * N + c0];
+            const int h1 = h + t + b;
+            if (h1 >= -t && h1 < N) acc += f[(size_t)(h1 + off) * N + c1];
+        }
+        dst[slot * S + rem] = acc;
+    }
+}
+
+// adjoint value of level m at input position (h, col) from level-m data g (rows h_out + 2w - 1)
+template <typename T> __device__ __forceinline__ T adj_at(const T* g, int N, int m, int h, int col) {
+    const int w = 1 << (m - 1);
+    const int l = col / (2 * w), r = col - l * 2 * w, c = r / w, t = r - c * w;
+    if (h < -t || h >= N) return 0;
+    const int base = l * 2 * w + 2 * t, off = 2 * w - 1;
+    if (c == 0) return g[(size_t)(h + off) * N + base] + g[(size_t)(h + off) * N + base + 1];
+    return g[(size_t)(h - t + off) * N + base] + g[(size_t)(h - t - 1 + off) * N + base + 1];
+}
+
+template <typename T>
+__global__ void adrt_adj_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S) {
+    const int N = 1 << n, w = 1 << (m - 1);
+    const int Hin = N + w - 1;
+    const size_t per = (size_t)Hin * N;
+    const size_t total = per * 4 * nimg;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t slot = e / per;
+        const size_t rem = e - slot * per;
+        const int row = (int)(rem >> n), col = (int)(rem & (N - 1));
+        dst[slot * S + rem] = adj_at(src + slot * S, N, m, row - (w - 1), col);
+    }
+}
+
+// level-1 adjoint of the four quadrants, T_q^T and the quadrant sum (adrtcore.py:131-137)
+template <typename T>
+__global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __restrict__ x, size_t S) {
+    const int N = 1 << n;
+    const size_t per = (size_t)N * N;
+    const size_t total = per * nimg;
+    for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+        const size_t img = e / per;
+        const size_t rem = e - img * per;
+        const int a = (int)(rem >> n), b = (int)(rem & (N - 1));
+        const T* g = src + img * 4 * S;
+        // x[a, b] = sum_q (T_q^T f_q)[a, b]: q0 f(N-1-b, a); q1 f(N-1-a, b); q2 f(a, b); q3 f(N-1-b, N-1-a)
+        T acc = adj_at(g + 0 * S, N, 1, N - 1 - b, a);
+        acc += adj_at(g + 1 * S, N, 1, N - 1 - a, b);
+        acc += adj_at(g + 2 * S, N, 1, a, b);
+        acc += adj_at(g + 3 * S, N, 1, N - 1 - b, N - 1 - a);
+        x[e] = acc;
+    }
+}
+
+template <typename T>
+static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st) {
+    const int N = 1 << n;
+    const size_t S = (size_t)(2 * N - 1) * N;
+    T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
+    const T* src = reinterpret_cast<const T*>(x);
+    for (int m = 1; m <= n; ++m) {
+        T* dst = (m == n) ? reinterpret_cast<T*>(b) : bufs[m & 1];
+        const size_t total = (size_t)(N + (1 << m) - 1) * N * 4 * nimg;
+        adrt_fwd_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S);
+        int rc = launch_status("adrt_fwd_level");
+        if (rc) return rc;
+        src = dst;
+    }
+    return ADRT_OK;
+}
+
+template <typename T>
+static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st) {
+    const int N = 1 << n;
+    const size_t S = (size_t)(2 * N - 1) * N;
+    T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
+    const T* src = reinterpret_cast<const T*>(b);
+    for (int m = n; m >= 2; --m) {
+        T* dst = bufs[m & 1];
+        const size_t total = (size_t)(N + (1 << (m - 1)) - 1) * N * 4 * nimg;
+        adrt_adj_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S);
+        int rc = launch_status("adrt_adj_level");
+        if (rc) return rc;
+        src = dst;
+    }
+    adrt_adj_final<T><<<grid_of((size_t)N * N * nimg), 256, 0, st>>>(n, nimg, src, reinterpret_cast<T*>(x), S);
+    return launch_status("adrt_adj_final");
+}
+
+int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st) {
+    if (n < 1 || n > 12 || nimg < 0) { set_error("adrt_forward: bad n=%d nimg=%d", n, nimg); return ADRT_EINVAL; }
+    if (!nimg) return ADRT_OK;
+    if (!x || !b || (!scratch && n > 1)) { set_error("adrt_forward: null pointer"); return ADRT_EINVAL; }
+    switch (dtype) {
+        case ADRT_F32: return fwd_t<float>(n, nimg, x, b, scratch, st);
+        case ADRT_F64: return fwd_t<double>(n, nimg, x, b, scratch, st);
+        case ADRT_I32: return fwd_t<int32_t>(n, nimg, x, b, scratch, st);
+        case ADRT_I64: return fwd_t<long long>(n, nimg, x, b, scratch, st);
+    }
+    set_error("adrt_forward: bad dtype %d", dtype);
+    return ADRT_EINVAL;
+}
+
+int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st) {
+    if (n < 1 || n > 12 || nimg < 0) { set_error("adrt_transpose: bad n=%d nimg=%d", n, nimg); return ADRT_EINVAL; }
+    if (!nimg) return ADRT_OK;
+    if (!x || !b || (!scratch && n > 1)) { set_error("adrt_transpose: null pointer"); return ADRT_EINVAL; }
+    switch (dtype) {
+        case ADRT_F32: return adj_t<float>(n, nimg, b, x, scratch, st);
+        case ADRT_F64: return adj_t<double>(n, nimg, b, x, scratch, st);
+        case ADRT_I32: return adj_t<int32_t>(n, nimg, b, x, scratch, st);
+        case ADRT_I64: return adj_t<long long>(n, nimg, b, x, scratch, st);
+    }
+    set_error("adrt_transpose: bad dtype %d", dtype);
+    return ADRT_EINVAL;
+}
+
+}  // namespace adrt

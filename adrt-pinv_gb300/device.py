@@ -1,0 +1,254 @@
+"""Device pipeline of the explicit oblique inverses (one GPU, stream-ordered, no host round trips).
+
+For a plan, a batch size B and a precision, `Pipeline` owns every device buffer and evaluates, for B images at once:
+  packed_image / packed_sino : fastops._packed (fastops.py:209-220) = pack+FFT kernel -> row engine -> iFFT+unpack
+  precond                    : the hybrid's P = g1_inv / lorr_inv (fasthybrid.py:108-130)
+  apply                      : backproject + fixed-degree outer Chebyshev (fastops.py:247-258, 283-288, 333-338)
+Layouts in HBM (per batch): Y (B, 2L, N) complex rows (pair (0,1) then (2,3), each L offset-frequency rows);
+three real image-space partial sums (3, B, N, N); outer state x, x_prev, y (B, N, N) in FP64 (or the compute
+precision in fp64 mode, where everything is FP64).
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _lib as C
+from .plan import Plan, outer_coeffs, roots_of_unity
+
+OPCODE = {"B": C.OP_B, "BT": C.OP_BT, "M": C.OP_M, "P": C.OP_P}
+PRECISIONS = {"fp32": torch.float32, "fp64": torch.float64}
+
+
+def fuse_ops(ops):
+    """Merge ('B', lo, hi) immediately followed by ('BT', lo, hi) into ('M', lo, hi) (one Gram application)."""
+    out = []
+    for op in ops:
+        op = (op[0], int(op[1]), int(op[2]))
+        if out and op[0] == "BT" and out[-1][0] == "B" and out[-1][1:] == op[1:]:
+            out[-1] = ("M", op[1], op[2])
+        else:
+            out.append(op)
+    return out
+
+
+def _cdtype(real):
+    return torch.complex64 if real == torch.float32 else torch.complex128
+
+
+class RowTables:
+    """Device copies of a plan's per-frequency tables in one precision, plus the work counter."""
+
+    def __init__(self, plan: Plan, real, device):
+        self.plan, self.real, self.device = plan, real, device
+        self.code = C.dtype_code(real)
+        self.roots = torch.from_numpy(roots_of_unity(plan.L)).to(device=device, dtype=_cdtype(real))
+        self.deg = torch.from_numpy(plan.deg.astype(np.int32)).to(device)
+        self.coef = torch.from_numpy(np.ascontiguousarray(plan.coef.ravel())).to(device=device, dtype=real)
+        self.rows_main = torch.from_numpy(plan.packed_rows(dense=False).astype(np.int32)).to(device)
+        self.rows_dense = torch.from_numpy(plan.packed_rows(dense=True).astype(np.int32)).to(device)
+        self.counter = torch.zeros(4, dtype=torch.int32, device=device)
+        self.F = None
+        if len(plan.dense_freqs):
+            tabs = plan.build_dense_tables()
+            idx = {int(k): i for i, k in enumerate(plan.dense_freqs)}
+            sel = [idx[int(r) % plan.L] for r in plan.packed_rows(dense=True)]
+            self.F = torch.from_numpy(tabs[sel]).to(device=device, dtype=_cdtype(real))
+        self.count = 0  # level-rows applied, counted as the reference does
+
+    def job(self, Y, ops, rows):
+        p = self.plan
+        B, R, N = Y.shape
+        j = C.RowJob()
+        j.dtype, j.n, j.nimg, j.nsel = self.code, p.n, B, int(rows.numel())
+        j.img_stride = R * N
+        j.X = Y.data_ptr()
+        j.rows = rows.data_ptr()
+        j.freq_mod = p.L
+        j.roots = self.roots.data_ptr()
+        j.twtab = None
+        j.deg = self.deg.data_ptr()
+        j.coef = self.coef.data_ptr()
+        j.coef_stride = p.coef_stride
+        j.tau = p.tau
+        if len(ops) > C.MAX_OPS:
+            raise ValueError("too many ops")
+        j.nops = len(ops)
+        for i, (op, lo, hi) in enumerate(ops):
+            j.op[i], j.lo[i], j.hi[i] = OPCODE[op], lo, hi
+        j.counter = self.counter.data_ptr()
+        j.grid = 0
+        return j
+
+    def run(self, Y, ops):
+        """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take their exact
+        filter as a batched matrix product in place of the polynomial (fastops.py:100-117)."""
+        ops = fuse_ops(ops)
+        B = Y.shape[0]
+        st = C.stream_handle()
+        pidx = [i for i, o in enumerate(ops) if o[0] == "P"]
+        if len(pidx) > 1:
+            raise ValueError("at most one filter op per list")
+        if self.F is None or not pidx:
+            rows = torch.cat([self.rows_main, self.rows_dense]) if self.F is not None else self.rows_main
+            C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, rows)), st)
+        else:
+            i = pidx[0]
+            pre, post = ops[:i], ops[i + 1 :]
+            C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, self.rows_main)), st)
+            if pre:
+                C.call("adrt_rows_run", ctypes.byref(self.job(Y, pre, self.rows_dense)), st)
+            rd = self.rows_dense.long()
+            Yd = Y.index_select(1, rd)  # (B, Kd2, N)
+            Zd = torch.bmm(self.F, Yd.permute(1, 2, 0))  # (Kd2, N, B)
+            Y.index_copy_(1, rd, Zd.permute(2, 0, 1))
+            if post:
+                C.call("adrt_rows_run", ctypes.byref(self.job(Y, post, self.rows_dense)), st)
+        self.count += B * self.plan.level_rows(ops_unfused(ops))
+
+
+def ops_unfused(ops):
+    out = []
+    for op, lo, hi in ops:
+        if op == "M":
+            out += [("B", lo, hi), ("BT", lo, hi)]
+        else:
+            out.append((op, lo, hi))
+    return out
+
+
+class Pipeline:
+    """Every device buffer for one (plan, batch size, precision)."""
+
+    def __init__(self, plan: Plan, batch, precision="fp32", device="cuda", stencil_precision=None):
+        if precision not in PRECISIONS:
+            raise ValueError(f"precision must be one of {tuple(PRECISIONS)}")
+        C.load()
+        self.plan, self.B, self.precision = plan, int(batch), precision
+        self.device = torch.device(device)
+        self.real = PRECISIONS[precision]
+        self.outer_real = torch.float64
+        self.stencil_real = PRECISIONS[stencil_precision or precision]
+        self.tables = RowTables(plan, self.real, self.device)
+        N, L, B = plan.N, plan.L, self.B
+        dev = self.device
+        self.Y = torch.empty((B, 2 * L, N), dtype=_cdtype(self.real), device=dev)
+        self.parts = torch.empty((3, B, N, N), dtype=self.real, device=dev)
+        self.xs = [torch.empty((B, N, N), dtype=self.outer_real, device=dev) for _ in range(3)]
+        self.y = torch.empty((B, N, N), dtype=self.outer_real, device=dev)
+        self.s = torch.empty((B, N, N), dtype=self.stencil_real, device=dev)
+        self.st = [torch.empty((B, N, N), dtype=self.stencil_real, device=dev) for _ in range(3)]
+        self.ops = _op_lists(plan)
+        self.launches = 0
+
+    # ---------------------------------------------------------------- packed passes
+    def _codes(self):
+        return C.dtype_code(self.real)
+
+    def packed_image(self, x, ops):
+        """fastops._packed with strips Tq(q, E x): x (B, N, N) real on device -> self.parts."""
+        p, st = self.plan, C.stream_handle()
+        C.call("adrt_pack_fft", self._codes(), p.n, self.B, 0, C.dtype_code(x.dtype), C.ptr(x), C.ptr(self.Y),
+               C.ptr(self.tables.roots), st)
+        self.tables.run(self.Y, ops)
+        self._unpack(st)
+        return self.parts
+
+    def packed_sino(self, b, ops):
+        """fastops._packed with strips iota(b_q): b (B, 4, 2N-1, N) real on device -> self.parts."""
+        p, st = self.plan, C.stream_handle()
+        C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1, C.dtype_code(b.dtype), C.ptr(b), C.ptr(self.Y),
+               C.ptr(self.tables.roots), st)
+        self.tables.run(self.Y, ops)
+        self._unpack(st)
+        return self.parts
+
+    def _unpack(self, st):
+        C.call("adrt_ifft_unpack", self._codes(), self.plan.n, self.B, C.ptr(self.Y), C.ptr(self.parts[0]),
+               C.ptr(self.parts[1]), C.ptr(self.parts[2]), C.ptr(self.tables.roots), st)
+
+    def sum_parts(self, out):
+        C.call("adrt_sum3", self._codes(), self.plan.n, self.B, C.ptr(self.parts[0]), C.ptr(self.parts[1]),
+               C.ptr(self.parts[2]), C.ptr(out), C.dtype_code(out.dtype), C.stream_handle())
+        return out
+
+    # ---------------------------------------------------------------- image-space steps
+    def resid(self, y, with_parts=True):
+        """s = y - (sum of the partial images) in the stencil precision (parts omitted: a cast of y)."""
+        p0, p1, p2 = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
+        C.call("adrt_resid", C.dtype_code(self.s.dtype), self.plan.n, self.B, C.dtype_code(y.dtype), C.ptr(y),
+               C.ptr(p0), C.ptr(p1), C.ptr(p2), C.ptr(self.s), C.stream_handle())
+        return self.s
+
+    def precond(self, s):
+        """Hybrid preconditioner P applied to s (fasthybrid.py:224-229): g1_inv (Chebyshev on [4, 16] of the G_1
+        stencil), lorr_inv, or the identity."""
+        p, st = self.plan, C.stream_handle()
+        code = C.dtype_code(s.dtype)
+        if p.precond == "none":
+            return s
+        if p.precond == "lorr":
+            out = self.st[0]
+            C.call("adrt_lorr", code, p.n, self.B, C.ptr(s), C.ptr(out), st)
+            return out
+        a, c, steps = outer_coeffs(4.0, 16.0, p.g1_deg)
+        bufs = self.st
+        C.call("adrt_g1_step", code, p.n, self.B, C.ptr(s), None, None, C.ptr(bufs[0]), 0.0, 0.0, a, st)
+        cur, prev = 0, None
+        for om_a, om_1 in steps:
+            nxt = 1 if cur != 1 and prev != 1 else (2 if cur != 2 and prev != 2 else 0)
+            C.call("adrt_g1_step", code, p.n, self.B, C.ptr(s), C.ptr(bufs[cur]),
+                   None if prev is None else C.ptr(bufs[prev]), C.ptr(bufs[nxt]), om_a, om_1, 0.0, st)
+            prev, cur = cur, nxt
+        return bufs[cur]
+
+    def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0):
+        C.call("adrt_outer_update", C.dtype_code(x_new.dtype), self.plan.n, self.B, C.ptr(x), C.ptr(x_prev), C.ptr(r),
+               C.dtype_code(r.dtype), C.ptr(x_new), om_a, om_1, a0, C.stream_handle())
+
+    # ---------------------------------------------------------------- operators
+    def G(self, x):
+        """The frame operator (L_p: frame_window, fastops.py:277-281) or G_h (hybrid, fastops.py:325-331) of x."""
+        return self.packed_image(x, self.ops["G"])
+
+    def backproject_into(self, b, y):
+        self.packed_sino(b, self.ops["BP"])
+        return self.sum_parts(y)
+
+    def apply(self, b):
+        """x = L b for B sinograms b (B, 4, 2N-1, N) on device; returns the FP64 (B, N, N) result buffer (a view
+        of internal storage, valid until the next call)."""
+        p = self.plan
+        if p.lo is None:
+            raise RuntimeError("plan has no outer interval")
+        a, c, steps = outer_coeffs(p.lo, p.hi, p.outer_deg)
+        y = self.backproject_into(b, self.y)
+        hybrid = p.method == "hybrid"
+        x, xp = self.xs[0], None
+        if hybrid:
+            r = self.precond(self.resid(y, with_parts=False))
+            self.outer_step(None, None, r, x, 0.0, 0.0, a)
+        else:
+            self.outer_step(None, None, y, x, 0.0, 0.0, a)
+        free = [self.xs[1], self.xs[2]]
+        for om_a, om_1 in steps:
+            self.G(x)
+            s = self.resid(y)
+            r = self.precond(s) if hybrid else s
+            xn = free.pop(0)
+            self.outer_step(x, xp, r, xn, om_a, om_1, 0.0)
+            if xp is not None:
+                free.append(xp)
+            xp, x = x, xn
+        return x
+
+
+def _op_lists(plan):
+    n = plan.n
+    if plan.method == "lp":  # fastops.py:277-285
+        return {"G": [("P", 1, n), ("B", 1, n), ("BT", 1, n)], "BP": [("BT", 1, n), ("P", 1, n)]}
+    return {  # fastops.py:325-335
+        "G": [("B", 1, 1), ("P", 2, n), ("B", 2, n), ("BT", 2, n), ("BT", 1, 1)],
+        "BP": [("BT", 2, n), ("P", 2, n), ("BT", 1, 1)],
+    }

@@ -1,0 +1,146 @@
+/* C ABI of the GB300 (sm_103a) implementation of the explicit oblique inverses of the ADRT.
+ *
+ * Two groups of entry points:
+ *  1. Drop-in replacements for the reference's native row kernels, cpp/oblique.cpp of dsrim/adrt-pinv, with the
+ *     same names, argument order and meaning (the reference binds them with ctypes at fastcpp.py:22-32). They
+ *     take HOST pointers, copy to the GPU, run the CUDA kernels and copy back before returning. The reference
+ *     returns void; these return an int status (0 = ok), which a binding with restype None simply ignores.
+ *     Complex arrays are interleaved (re, im) doubles, C-contiguous rows of N = 2^n values.
+ *  2. Device-pointer entry points used by the Python host (adrt-pinv_gb300/): stream-ordered, asynchronous,
+ *     no allocation inside (scratch comes from the caller), FP32 or FP64 data. `stream` is a cudaStream_t
+ *     passed as void* (NULL = legacy default stream).
+ * All functions return ADRT_OK or an error code; adrt_last_error() gives a message for the calling thread.
+ */
+#ifndef ADRT_PINV_GB300_H
+#define ADRT_PINV_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ADRT_OK 0
+#define ADRT_EINVAL 1       /* bad argument (shape, range, null pointer) */
+#define ADRT_ECUDA 2       /* CUDA runtime or launch error */
+#define ADRT_ENOMEM 3      /* device allocation failed */
+#define ADRT_EUNSUPPORTED 4
+
+#define ADRT_F32 0
+#define ADRT_F64 1
+#define ADRT_I32 2
+#define ADRT_I64 3
+
+/* row-program operations (the op lists of fastops.RowEngine.run, fastops.py:156-167) */
+#define ADRT_OP_B 0  /* forward butterflies B_hi ... B_lo */
+#define ADRT_OP_BT 1 /* adjoint butterflies */
+#define ADRT_OP_M 2  /* B then BT over the same levels (M = B^* B) */
+#define ADRT_OP_P 3  /* Chebyshev filter p_k(M) over levels lo..hi */
+#define ADRT_MAX_OPS 8
+
+/* ------------------------------------------------------------------ 1. reference drop-ins (host pointers) */
+
+/* cpp/oblique.cpp:56 bfly_rows: X (K x N complex) in place; transpose = 0: B_{m_hi}...B_{m_lo}, 1: adjoint.
+ * z: K complex frequencies z_k. nthreads is accepted and ignored (the GPU supplies the parallelism). */
+int bfly_rows(int n, int K, const double* z, double* X, int m_lo, int m_hi, int transpose, int nthreads);
+
+/* cpp/oblique.cpp:74 cheb_rows: Z[k] = p_k(M) Y[k] with deg[k] Chebyshev steps, constants a[k], c[k]
+ * (fastspec.cheb_coeffs), shift tau, M = B^* B over levels m_lo..m_hi. steps (nullable) += level-rows applied. */
+int cheb_rows(int n, int K, const double* z, const int* deg, const double* a, const double* c, double tau,
+              const double* Y, double* Z, int m_lo, int m_hi, int nthreads, long long* steps);
+
+/* cpp/oblique.cpp:108 cert_rowsum: certified bounds Lambda_k >= lambda_max(M_k), levels m_lo..n, K frequencies. */
+int cert_rowsum(int n, int K, const double* omega, int m_lo, double* out, int nthreads);
+
+/* cpp/oblique.cpp:132 omp_max_threads: here the number of SMs of the current device (the row parallelism). */
+int omp_max_threads(void);
+
+/* message of the last error on the calling thread ("" if none) */
+const char* adrt_last_error(void);
+/* library ABI version */
+int adrt_abi_version(void);
+
+/* ------------------------------------------------------------------ 2. device entry points */
+
+/* One launch of the row engine over nimg images x nsel selected rows (fastops.RowEngine.run /
+ * fastcpp.CppEngine._B/_BT/_P, fastops.py:70-167, fastcpp.py:62-99). Every selected row runs the same op list.
+ * Rows are processed in the given order (callers sort by cost, descending) by persistent warps that take work
+ * from *counter; the call resets *counter to 0 on the stream before the launch. Rows are read and written in
+ * natural (logical) order whatever the op list. */
+typedef struct adrt_row_job {
+    int dtype;              /* ADRT_F32 / ADRT_F64: precision of X, twiddles and coefficients */
+    int n;                  /* N = 2^n values per row, 1 <= n <= 11 */
+    int nimg;               /* images in the batch */
+    int nsel;               /* selected rows per image */
+    int64_t img_stride;     /* complex elements between consecutive images of X */
+    void* X;                /* rows (complex interleaved, row stride N), transformed in place */
+    const int32_t* rows;    /* nsel row indices (row r of image b is X + b*img_stride + r*N) */
+    int freq_mod;           /* frequency index of row r: k = r % freq_mod */
+    const void* roots;      /* twiddle mode 0: L = 2N roots of unity exp(2 pi i j / L) (z_k = root[k]), or NULL */
+    const void* twtab;      /* twiddle mode 1 (roots == NULL): per-row table z^t, t = 0..N/2, row stride N/2+1 */
+    const int32_t* deg;     /* per frequency inner degree d_k (ADRT_OP_P) */
+    const void* coef;       /* per frequency: a_k, then (omega_j, omega_j a_k, omega_j - 1) for j = 1..d_k-1 */
+    int coef_stride;        /* elements per frequency in coef */
+    double tau;             /* Tikhonov shift of the filter */
+    int nops;
+    int op[ADRT_MAX_OPS], lo[ADRT_MAX_OPS], hi[ADRT_MAX_OPS];
+    int32_t* counter;       /* device int used as the work counter */
+    int grid;               /* persistent CTAs (0 = one per SM) */
+} adrt_row_job;
+
+int adrt_rows_run(const adrt_row_job* job, void* stream);
+
+/* Per-row twiddle table tab[k*(N/2+1) + t] = z_k^t (t = 0..N/2) from K complex z (FP64 in, dtype out),
+ * by binary powering in FP64. */
+int adrt_twiddle_table(int dtype, int n, int K, const double* z, void* tab, void* stream);
+
+/* Power iteration for Lambda_k (fastcpp.py:102-118): V (K x N, dtype) is iterated `iters` times
+ * V <- M V / ||M V|| row-wise (M = B^* B over levels m_lo..n) and out[k] = safety * Re <V_k, M V_k> (FP64 out).
+ * Twiddles from the K x (N/2+1) table twtab. */
+int adrt_power_rows(int dtype, int n, int K, void* V, const void* twtab, int m_lo, int iters, double safety,
+                    double* out, int32_t* counter, void* stream);
+
+/* cert_rowsum on device pointers (cpp/oblique.cpp:108-130). */
+int adrt_cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, void* stream);
+
+/* Quadrant packing + FFT along the offset axis (fastops._packed, fastops.py:209-214): for each image, the two
+ * pairs (0,1), (2,3) of quadrant strips s_qa + i s_qb are transformed with a length L = 2N DFT along axis 0 into
+ * Y (nimg x 2L x N complex, dtype). src_kind 0: src is nimg images N x N (real, src_dtype), strips = Tq(q, E x)
+ * (fastspec.py:142-152); src_kind 1: src is nimg sinograms 4 x (2N-1) x N, strips = iota(b_q) (fastspec.py:170-174).
+ * roots: L roots of unity in dtype. */
+int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
+                  void* stream);
+
+/* Inverse FFT along the offset axis + unpacking (fastops.py:216-220): from Z (nimg x 2L x N complex) produce the
+ * three image-space partial sums whose total is E^T sum_q T_q^T Re/Im(ifft Z) (fastspec.py:154-168):
+ * colpart (quadrants II, III), rowpart0 (quadrant I) and rowpart3 (quadrant IV), each nimg x N x N, dtype real. */
+int adrt_ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* rowpart0, void* rowpart3,
+                     const void* roots, void* stream);
+
+/* Image-space kernels on nimg N x N images (dtype = ADRT_F32 / ADRT_F64 for all image arguments).
+ * resid:   s = y - (p0 + p1 + p2)  (y in ydtype; parts in dtype, all NULL = 0, which casts y; s in dtype)
+ * g1_step: one step of cheb_solve(G1_apply, s, 4, 16, deg) (fasthybrid.py:95-130): with G1 x = 8x + J K x + (J K x^T)^T,
+ *          xn = x + om_a*(s - G1 x) + om_1*(x - xp); first step (xp == NULL, x == NULL): xn = a*s.
+ * lorr:    out = (s - Pi s)/4 + Pi s/12 (fasthybrid.py:101-111).
+ * outer:   x_new = x + om_a * r + om_1 * (x - x_prev) (fastops.py:247-258); x, x_prev, x_new in dtype, r in
+ *          rdtype (no wider than dtype); x == NULL: x_new = a0 * r; x_prev == NULL: zero. */
+int adrt_resid(int dtype, int n, int nimg, int ydtype, const void* y, const void* p0, const void* p1, const void* p2,
+               void* s, void* stream);
+int adrt_g1_step(int dtype, int n, int nimg, const void* s, const void* x, const void* xp, void* xn, double om_a,
+                 double om_1, double a0, void* stream);
+int adrt_lorr(int dtype, int n, int nimg, const void* s, void* out, void* stream);
+int adrt_outer_update(int dtype, int n, int nimg, const void* x, const void* x_prev, const void* r, int rdtype,
+                      void* x_new, double om_a, double om_1, double a0, void* stream);
+int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const void* p2, void* out, int out_dtype,
+              void* stream);
+
+/* Spatial ADRT in the reference's sinogram layout (adrtcore.py:122-137), nimg images, exact for integer dtypes
+ * (ADRT_I32, ADRT_I64; sums only), FP32 / FP64 otherwise. scratch: 2 * nimg * 4 * (2N-1) * N elements of dtype.
+ * forward: x (nimg x N x N) -> b (nimg x 4 x (2N-1) x N); transpose: b -> x. */
+int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scratch, void* stream);
+int adrt_transpose(int dtype, int n, int nimg, const void* b, void* x, void* scratch, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,132 @@
+"""GPU inverses (FastLpGpu / FastHybridGpu) against the reference's golden outputs and the CPU oracle.
+
+Tolerances: FP64 mode <= 1e-12 (operators) / 1e-11 (apply) relative, as the reference's own engines agree;
+FP32 mode <= 1e-5 relative error vs FP64 (the benchmark spec's bound)."""
+
+import numpy as np
+import pytest
+
+from conftest import max_rel, rel_err
+from oracle import cpu_engine as CE
+from oracle import oblique_np as O
+
+pytestmark = pytest.mark.gpu
+
+CASES = [("lp", {}), ("hyb", {}), ("hybd8", {"dense_cap": 8}), ("lpd8", {"dense_cap": 8}),
+         ("hyblorr", {"precond": "lorr"})]
+
+
+def _cls(pkg, name):
+    return pkg.FastHybridGpu if name.startswith("hyb") else pkg.FastLpGpu
+
+
+@pytest.mark.parametrize("n", [4, 6])
+@pytest.mark.parametrize("name,kw", CASES)
+def test_fp64_matches_reference(pkg, golden, n, name, kw):
+    k = f"{name}_{n}"
+    P = _cls(pkg, name)(n, lam_max=golden[f"inv_lam_{k}"], outer=tuple(golden[f"inv_outer_{k}"]), precision="fp64", **kw)
+    assert np.array_equal(P.deg, golden[f"inv_deg_{k}"])
+    x, b = golden[f"inv_x_{n}"], golden[f"inv_b_{n}"]
+    G = P.Gh if name.startswith("hyb") else P.frame_window
+    assert max_rel(G(x), golden[f"inv_G_{k}"]) < 1e-12
+    assert max_rel(P.backproject(b), golden[f"inv_bp_{k}"]) < 1e-12
+    P.eng.count = [0]
+    xr = P.apply(b)
+    assert max_rel(xr, golden[f"inv_apply_{k}"]) < 1e-11
+    assert P.eng.count[0] == int(golden[f"inv_count_{k}"])
+
+
+def test_config0_lp_fp64_p16(pkg, golden):
+    """L_p, FP64, N=64, p=16 on the noisy ellipse phantom: <= 1e-12 vs the reference's C++ engine."""
+    P = pkg.FastLpGpu(6, lam_max=golden["c0_lam"], deg_cap=16, outer=tuple(golden["c0_outer"]), precision="fp64")
+    assert np.array_equal(P.deg, golden["c0_deg"])
+    assert rel_err(P.backproject(golden["c0_b"]), golden["c0_bp"]) < 1e-12
+    assert rel_err(P.apply(golden["c0_b"]), golden["c0_apply"]) < 1e-12
+
+
+@pytest.mark.parametrize("name,kw", CASES)
+def test_fp32_within_1e5(pkg, golden, name, kw):
+    n = 6
+    k = f"{name}_{n}"
+    P = _cls(pkg, name)(n, lam_max=golden[f"inv_lam_{k}"], outer=tuple(golden[f"inv_outer_{k}"]), precision="fp32", **kw)
+    assert rel_err(P.apply(golden[f"inv_b_{n}"]), golden[f"inv_apply_{k}"]) < 1e-5
+
+
+def test_packed_roundtrip_property(pkg):
+    """With an empty row op list the packed pass is sum_q TqT(ifft(fft(Tq x))) = 4x (FFT round trip, Tq unitary)."""
+    import torch
+
+    for prec, tol in (("fp64", 1e-13), ("fp32", 1e-6)):
+        for n in (3, 7, 9):
+            N = 1 << n
+            plan = pkg.Plan("lp", n, np.full(2 * N, 4.0), outer=(1.0, 2.0, 3))
+            pipe = pkg.Pipeline(plan, 2, prec)
+            x = torch.randn(2, N, N, dtype=torch.float64, device="cuda")
+            pipe.packed_image(x, [])
+            out = torch.empty_like(x)
+            pipe.sum_parts(out)
+            assert torch.max(torch.abs(out - 4 * x)).item() / torch.max(torch.abs(x)).item() < tol
+
+
+def test_packed_sino_matches_oracle(pkg):
+    import torch
+
+    n = 5
+    N = 1 << n
+    rng = np.random.default_rng(2)
+    b = rng.standard_normal((4, 2 * N - 1, N))
+    plan = pkg.Plan("lp", n, np.full(2 * N, 4.0), outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, 1, "fp64")
+    pipe.packed_sino(torch.from_numpy(b[None]).cuda(), [])
+    out = torch.empty((1, N, N), dtype=torch.float64, device="cuda")
+    pipe.sum_parts(out)
+
+    class Ident:
+        def run(self, Y, ops):
+            return Y
+
+    ref = O.packed(n, Ident(), lambda q: O.iota(n, b[q]), [])
+    assert max_rel(out[0].cpu().numpy(), ref) < 1e-13
+
+
+@pytest.fixture(scope="module")
+def hybrid256(pkg):
+    """N=256, p=32 hybrid with its plan computed on the GPU (power iteration + Lanczos)."""
+    return pkg.FastHybridGpu(8, deg_cap=32, precision="fp32")
+
+
+def test_n256_hybrid_fp32_vs_cpu_reference_engine(pkg, hybrid256):
+    """N=256, p=32, FP32 on a noisy ellipse phantom: <= 1e-5 vs the FP64 C++-engine path on the same plan."""
+    H = hybrid256
+    n, N = 8, 256
+    x = pkg.phantoms.ellipse_phantom(N, seed=7)
+    b = pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, x), 1e-3, seed=8)
+    xg = H.apply(b)
+    ref = CE.hybrid_cpu(n, dict(lam_max=H.lam_max, deg=H.deg, outer=(H.lo, H.hi, H.outer_deg)), threads=16).apply(b)
+    assert rel_err(xg, ref) < 1e-5
+    assert rel_err(xg, x) < 0.05  # noisy data: close to the phantom
+
+
+def test_n256_left_inverse_and_linearity(pkg, hybrid256):
+    import torch
+
+    H = hybrid256
+    n, N = 8, 256
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal((2, N, N))
+    b = pkg.adrtcore.adrt(n, x)
+    xr = H.apply(b)
+    assert rel_err(xr[0], x[0]) < 1e-5 and rel_err(xr[1], x[1]) < 1e-5  # L R x = x
+    bt = torch.from_numpy(b).cuda()
+    lin = H.apply(bt[0] + 2.0 * bt[1]).cpu().numpy()
+    assert rel_err(lin, xr[0] + 2.0 * xr[1]) < 1e-5
+
+
+def test_batch_equals_single(pkg, hybrid256):
+    """Each result is the same alone and inside a batch (bit-identical: no cross-image arithmetic)."""
+    n, N = 8, 256
+    bs = np.stack([pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, pkg.phantoms.ellipse_phantom(N, seed=s)), 1e-3, seed=s + 100)
+                   for s in range(3)])
+    batch = hybrid256.apply(bs)
+    for i in range(3):
+        assert np.array_equal(batch[i], hybrid256.apply(bs[i]))
