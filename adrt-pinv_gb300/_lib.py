@@ -53,6 +53,8 @@ PROTOTYPES = {
     "omp_max_threads": [],
     "adrt_last_error": [],
     "adrt_abi_version": [],
+    "adrt_launch_count": [],
+    "adrt_fp32_probe": [_I, _I, _I, _P, _P],
     "adrt_rows_run": [ctypes.POINTER(RowJob), _P],
     "adrt_twiddle_table": [_I, _I, _I, _P, _P, _P],
     "adrt_power_rows": [_I, _I, _I, _P, _P, _I, _I, _D, _P, _P, _P],
@@ -82,7 +84,7 @@ def load(path=LIB_PATH):
     for name, args in PROTOTYPES.items():
         fn = getattr(lib, name)
         fn.argtypes = args
-        fn.restype = ctypes.c_char_p if name == "adrt_last_error" else ctypes.c_int
+        fn.restype = {"adrt_last_error": ctypes.c_char_p, "adrt_launch_count": ctypes.c_longlong}.get(name, ctypes.c_int)
     _lib = lib
     return lib
 

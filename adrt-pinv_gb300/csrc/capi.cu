@@ -1,4 +1,5 @@
 // extern "C" entry points of libadrt_pinv_gb300.so (declared in include/adrt_pinv_gb300.h).
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -26,7 +27,13 @@ int cuda_status(cudaError_t e, const char* where) {
     return e == cudaErrorMemoryAllocation ? ADRT_ENOMEM : ADRT_ECUDA;
 }
 
-int launch_status(const char* where) { return cuda_status(cudaGetLastError(), where); }
+static std::atomic<long long> g_launches{0};
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int launch_status(const char* where) {
+    count_launch();
+    return cuda_status(cudaGetLastError(), where);
+}
 
 int ensure_smem(const void* func, size_t bytes) {
     static std::mutex mu;
@@ -117,6 +124,7 @@ using namespace adrt;
 extern "C" {
 
 const char* adrt_last_error(void) { return g_err; }
+long long adrt_launch_count(void) { return g_launches.load(); }
 int adrt_abi_version(void) { return 1; }
 
 int omp_max_threads(void) { return device_sm_count(); }
@@ -268,6 +276,32 @@ int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scrat
 
 int adrt_transpose(int dtype, int n, int nimg, const void* b, void* x, void* scratch, void* stream) {
     return adrt_adj(dtype, n, nimg, b, x, scratch, as_stream(stream));
+}
+
+// FP32 FMA throughput probe: every thread runs `iters` rounds of 8 independent FMA chains (16 flop per chain and
+// round); out receives one value per thread so the work cannot be elided.
+__global__ void fma_probe_kernel(int iters, float seed, float* out) {
+    float a[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) a[i] = seed + threadIdx.x * 1e-7f + i;
+    const float m = 0.999999f, c = 1e-7f;
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+        for (int r = 0; r < 8; ++r) {
+#pragma unroll
+            for (int i = 0; i < 8; ++i) a[i] = fmaf(a[i], m, c);
+        }
+    }
+    float s = 0;
+#pragma unroll
+    for (int i = 0; i < 8; ++i) s += a[i];
+    out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+int adrt_fp32_probe(int blocks, int threads, int iters, float* out, void* stream) {
+    if (blocks < 1 || threads < 32 || threads > 1024 || iters < 1 || !out) { set_error("fp32_probe: bad arguments"); return ADRT_EINVAL; }
+    fma_probe_kernel<<<blocks, threads, 0, as_stream(stream)>>>(iters, 1.0f, out);
+    return launch_status("fma_probe_kernel");
 }
 
 }  // extern "C"

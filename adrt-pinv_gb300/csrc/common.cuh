@@ -64,4 +64,7 @@ int launch_status(const char* where);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// number of kernels this library has launched (all threads), for launch accounting
+void count_launch();
+
 }  // namespace adrt

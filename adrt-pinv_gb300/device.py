@@ -49,13 +49,12 @@ class RowTables:
         self.rows_main = torch.from_numpy(plan.packed_rows(dense=False).astype(np.int32)).to(device)
         self.rows_dense = torch.from_numpy(plan.packed_rows(dense=True).astype(np.int32)).to(device)
         self.counter = torch.zeros(4, dtype=torch.int32, device=device)
-        self.F = None
-        if len(plan.dense_freqs):
-            tabs = plan.build_dense_tables()
-            idx = {int(k): i for i, k in enumerate(plan.dense_freqs)}
-            sel = [idx[int(r) % plan.L] for r in plan.packed_rows(dense=True)]
-            self.F = torch.from_numpy(tabs[sel]).to(device=device, dtype=_cdtype(real))
+        # dense rows: row r of the dense selection uses frequency table index dense_idx[r]
+        idx = {int(k): i for i, k in enumerate(plan.dense_freqs)}
+        self.dense_sel = np.array([idx[int(r) % plan.L] for r in plan.packed_rows(dense=True)], dtype=np.int64)
+        self._dense_dev = {}
         self.count = 0  # level-rows applied, counted as the reference does
+        self.timer = None  # list: when set, (start, end) CUDA events of every polynomial-row launch are appended
 
     def job(self, Y, ops, rows):
         p = self.plan
@@ -81,27 +80,72 @@ class RowTables:
         j.grid = 0
         return j
 
+    def _timed_main(self, Y, ops, st):
+        if self.timer is None:
+            C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, self.rows_main)), st)
+            return
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, self.rows_main)), st)
+        e1.record()
+        self.timer.append((e0, e1, ops))
+
+    def main_level_rows(self, ops):
+        """Level-rows processed by the polynomial-row launch of one op list (the dense rows excluded)."""
+        p = self.plan
+        n_main = int(self.rows_main.numel())
+        d = np.tile(p.deg, 2)[p.packed_rows(dense=False)]
+        tot = 0
+        for op, lo, hi in ops_unfused(fuse_ops(ops)):
+            if op in ("B", "BT"):
+                tot += n_main * (hi - lo + 1)
+            elif op == "P":
+                tot += int(np.sum(np.maximum(d - 1, 0))) * 2 * (hi - lo + 1)
+        return tot
+
+    def dense_table(self, fold_pre, fold_post):
+        key = (fold_pre, fold_post)
+        if key not in self._dense_dev:
+            T = self.plan.dense_operator(fold_pre, fold_post)
+            self._dense_dev[key] = torch.from_numpy(T[self.dense_sel]).to(device=self.device, dtype=_cdtype(self.real))
+        return self._dense_dev[key]
+
     def run(self, Y, ops):
-        """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take their exact
-        filter as a batched matrix product in place of the polynomial (fastops.py:100-117)."""
+        """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take the exact
+        filter (fastops.py:100-117), fused with the adjoint levels before it and the Gram levels after it into one
+        precomputed operator applied as a batched matrix product."""
         ops = fuse_ops(ops)
         B = Y.shape[0]
+        if not ops:
+            return
         st = C.stream_handle()
         pidx = [i for i, o in enumerate(ops) if o[0] == "P"]
         if len(pidx) > 1:
             raise ValueError("at most one filter op per list")
-        if self.F is None or not pidx:
-            rows = torch.cat([self.rows_main, self.rows_dense]) if self.F is not None else self.rows_main
-            C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, rows)), st)
+        dense = len(self.plan.dense_freqs) > 0
+        if not dense or not pidx:
+            if dense:
+                rows = torch.cat([self.rows_main, self.rows_dense])
+                C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, rows)), st)
+            else:
+                self._timed_main(Y, ops, st)
         else:
             i = pidx[0]
-            pre, post = ops[:i], ops[i + 1 :]
-            C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, self.rows_main)), st)
+            _, plo, phi = ops[i]
+            pre, post = list(ops[:i]), list(ops[i + 1 :])
+            fold_pre = bool(pre) and pre[-1] == ("BT", plo, phi)
+            if fold_pre:
+                pre = pre[:-1]
+            fold_post = bool(post) and post[0] == ("M", plo, phi)
+            if fold_post:
+                post = post[1:]
+            self._timed_main(Y, ops, st)
             if pre:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, pre, self.rows_dense)), st)
+            T = self.dense_table(fold_pre, fold_post)
             rd = self.rows_dense.long()
-            Yd = Y.index_select(1, rd)  # (B, Kd2, N)
-            Zd = torch.bmm(self.F, Yd.permute(1, 2, 0))  # (Kd2, N, B)
+            Yd = Y.index_select(1, rd)  # (B, 2Kd, N)
+            Zd = torch.bmm(T, Yd.permute(1, 2, 0))  # (2Kd, N, B)
             Y.index_copy_(1, rd, Zd.permute(2, 0, 1))
             if post:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, post, self.rows_dense)), st)

@@ -102,7 +102,7 @@ class _GpuInverse:
         self.plan = Plan(self.method, n, lam_max, tau_fac, eps_in, eps, deg_cap=deg_cap, dense_cap=dense_cap,
                          precond=precond, g1_deg=g1_deg)
         self.lam_max, self.deg = self.plan.lam_max, self.plan.deg
-        self.eng = EngineInfo(2 * len(self.plan.dense_freqs) // 2)
+        self.eng = EngineInfo(len(self.plan.dense_freqs))
         self._pipes = {}
         if outer is None:
             outer = self._outer_interval(eps)
@@ -187,24 +187,31 @@ class _GpuInverse:
         self._count(pipe, before)
         return out[0].cpu().numpy()
 
-    def apply(self, b):
-        """x = L b (fastops.py:287-288 / 337-338) for one sinogram or a batch; see the module docstring."""
+    def apply(self, b, out=None):
+        """x = L b (fastops.py:287-288 / 337-338) for one sinogram or a batch; see the module docstring.
+        out: optional result buffer (torch, host or device) written with a stream-ordered copy and returned."""
         is_torch = isinstance(b, torch.Tensor)
         bt = b if is_torch else torch.from_numpy(np.ascontiguousarray(np.asarray(b, dtype=np.float64)))
         single = bt.dim() == 3
         if single:
             bt = bt.unsqueeze(0)
-        if bt.shape[1:] != (4, 2 * self.N - 1, self.N):
+        if tuple(bt.shape[1:]) != (4, 2 * self.N - 1, self.N):
             raise ValueError(f"sinograms must have shape (4, {2 * self.N - 1}, {self.N})")
         if bt.dtype not in (torch.float32, torch.float64):
             bt = bt.double()
+        host_in = not bt.is_cuda
         bt = bt.to(self.device, non_blocking=True).contiguous()
         pipe = self.pipeline(bt.shape[0])
         before = pipe.tables.count
         x = pipe.apply(bt)
         self._count(pipe, before)
-        out = x.clone() if is_torch else x.cpu().numpy()
-        return out[0] if single else out
+        x = x[0] if single else x
+        if out is not None:
+            out.copy_(x, non_blocking=True)
+            return out
+        if not is_torch:
+            return x.cpu().numpy()
+        return x.to("cpu") if host_in else x.clone()
 
 
 class FastLpGpu(_GpuInverse):

@@ -159,13 +159,41 @@ class Plan:
         lo, hi = self.p_levels
         z = roots_of_unity(self.L)
         out = np.empty((len(self.dense_freqs), N, N), dtype=complex)
+        self._dense_eig = []
         for i, k in enumerate(self.dense_freqs):
             A = _butterfly_matrix(n, z[k], lo, hi)
             lam, V = np.linalg.eigh(A.conj().T @ A)
             lam = np.maximum(lam, 0)
             out[i] = (V / (lam + self.tau)) @ V.conj().T
+            self._dense_eig.append((A, lam, V))
         self.dense_tables = out
         return out
+
+    def dense_operator(self, fold_pre_adjoint, fold_post_gram):
+        """Per dense frequency, the exact operator that replaces the filter op of an op list together with the
+        butterflies around it: F_k, F_k A_k^* (filter after the adjoint levels, as in the back-projections) or
+        M_k F_k = V diag(lambda/(lambda+tau)) V^* (filter then M, as in G_h and the frame operator). In exact
+        arithmetic these equal the reference's dense-row path (fastops.py:100-117) followed / preceded by the
+        butterflies; evaluated once in FP64 they keep the ill-conditioned low-frequency rows accurate when the
+        rest of the pipeline runs in FP32. (Kd, N, N) complex, FP64."""
+        self.build_dense_tables()
+        key = (bool(fold_pre_adjoint), bool(fold_post_gram))
+        cache = self.__dict__.setdefault("_dense_ops", {})
+        if key in cache:
+            return cache[key]
+        mats = []
+        for (A, lam, V), F in zip(self._dense_eig, self.dense_tables):
+            if key == (False, True):
+                T = (V * (lam / (lam + self.tau))) @ V.conj().T
+            elif key == (True, False):
+                T = F @ A.conj().T
+            elif key == (True, True):
+                T = (V * (lam / (lam + self.tau))) @ V.conj().T @ A.conj().T
+            else:
+                T = F
+            mats.append(T)
+        cache[key] = np.array(mats) if mats else None
+        return cache[key]
 
     # ---------------------------------------------------------------- cache
     def save(self, path):

@@ -1,0 +1,319 @@
+"""Benchmark: batched hybrid inverse of the ADRT at N=256 on one GB300 (replicas across GPUs).
+
+Workload (one step): the hybrid explicit inverse (fastops.FastHybrid.apply semantics) of a batch of 64 noisy
+sinograms of seeded 10-ellipse phantoms at N = 256 (n = 8), inner degrees capped at p = 32, dense low-frequency
+table for d_k > 16, FP32 row engine / FFTs / stencil with FP64 tables and FP64 outer iteration. Metric: whole-job
+reconstructions per second. Every step's inputs (268 MB of FP64 sinograms) exceed the 129 MB L2, so no flush is
+needed between steps.
+
+  value : device-resident sinograms, K timed steps of Pipeline.apply (CUDA events, barrier + sync both sides).
+  e2e   : the public API FastHybridGpu.apply on pinned host sinograms with the result read back to pinned host
+          memory every step (H2D + D2H inside the timed region).
+  roofline : the row engine (rows_fast_kernel), the dominant kernel, timed live with CUDA events on its stream;
+          algorithmic FLOPs = level-rows x 8N (the reference's cost unit, fastops.py:166); peak = FP32 FMA
+          throughput measured in this run by the library's probe kernel.
+  cpu_baseline : the reference's C++-engine path (FastHybridCpp semantics: C row kernels + NumPy) timed on this
+          host's cores on one image of the same workload, same plan.
+`--impl reference` times only that CPU path (rank 0) on the same config and prints its own line.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+N_LOG2, BATCH, P_CAP, DENSE_CAP, REL_SIGMA = 8, 64, 32, 16, 1e-3
+METRIC = "hybrid-inverse recon/s at N=256 (<=1e-5 vs FP64)"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=BATCH)
+    ap.add_argument("--n", type=int, default=N_LOG2)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile-region", action="store_true", help="cudaProfilerStart/Stop around the timed steps")
+    return ap.parse_args()
+
+
+def config(args, world):
+    N = 1 << args.n
+    return {"workload": f"hybrid inverse, N={N}, batch {args.batch} per GPU, p={P_CAP}, dense_cap={DENSE_CAP}, "
+                        f"10-ellipse phantoms + noise {REL_SIGMA:g} max|b|",
+            "N": N, "global_batch": args.batch * world, "p": P_CAP, "dense_cap": DENSE_CAP, "method": "hybrid",
+            "precond": "g1", "precision": "fp32 rows/FFT/stencil, fp64 tables and outer state",
+            "parallelism": f"replicas x{world}", "l2": "inputs (268 MB/step) larger than L2; no flush"}
+
+
+def sinograms(pkg, n, B, seed0, device):
+    """Seeded phantoms -> ADRT on the GPU (FP64) -> i.i.d. noise sigma = 1e-3 max|b| (per sinogram)."""
+    import torch
+
+    N = 1 << n
+    xs = np.stack([pkg.phantoms.ellipse_phantom(N, seed=seed0 + i) for i in range(B)])
+    b = pkg.adrtcore.adrt(n, torch.from_numpy(xs).to(device))
+    g = torch.Generator(device=device).manual_seed(seed0)
+    noise = torch.randn(b.shape, generator=g, device=device, dtype=b.dtype)
+    return b + REL_SIGMA * b.abs().amax(dim=(1, 2, 3), keepdim=True) * noise
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx, self.rows, self.proc = str(gpu_index), [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", self.idx], stdout=subprocess.PIPE, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait(timeout=5)
+
+    def summary(self):
+        sm = [float(r[1]) for r in self.rows if len(r) >= 9 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) >= 9 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows if len(r) >= 9 for i in range(4) if r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(sm)}
+
+
+def fp32_peak(pkg, torch):
+    """FP32 FLOP/s of the library's FMA probe kernel (8 independent chains per thread, all SMs)."""
+    C = pkg._lib
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    blocks, threads, iters = sms * 8, 256, 4000
+    out = torch.empty(blocks * threads, dtype=torch.float32, device="cuda")
+    st = C.stream_handle()
+    for _ in range(2):
+        C.call("adrt_fp32_probe", blocks, threads, 200, C.ptr(out), st)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    best = 0.0
+    for _ in range(3):
+        e0.record()
+        C.call("adrt_fp32_probe", blocks, threads, iters, C.ptr(out), st)
+        e1.record()
+        torch.cuda.synchronize()
+        best = max(best, blocks * threads * iters * 128 / (e0.elapsed_time(e1) * 1e-3))
+    return best
+
+
+def cpu_reference_time(n, plan_kw, b_one, reps, threads):
+    """Seconds per apply of the reference's C++-engine path on the host (oracle/_ref when built, else the port)."""
+    from oracle import cpu_engine as CE
+
+    H = CE.hybrid_cpu(n, plan_kw, threads=threads)
+    H.apply(b_one)  # warm-up (and the dense tables)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        H.apply(b_one)
+        ts.append(time.perf_counter() - t0)
+    return min(ts), H.eng.kind
+
+
+def traffic_per_launch():
+    """DRAM bytes per launch of the row kernel from the committed ncu summary (null when not captured)."""
+    path = os.path.join(REPO, "profiles", "rows_fast_kernel_hybrid_n8_b64.txt")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch:"):
+                return float(line.split(":", 1)[1])
+    except OSError:
+        pass
+    return None
+
+
+def run_reference(args):
+    """CPU reference arm: the reference's C++ row kernels + NumPy glue on the host cores, same workload."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    from oracle import adrt_np as A
+    from oracle import cpu_engine as CE
+    from oracle import oblique_np as O
+
+    n, N = args.n, 1 << args.n
+    threads = os.cpu_count() or 1
+    os.environ.setdefault("OPENBLAS_NUM_THREADS", "1")
+    CE.build()
+    # the reference's own setup on the CPU: power iteration (fastcpp conventions), degrees capped at p, Lanczos
+    lam = O.power_lam_max(n, O.offset_z(2 * N), 2, seeds=(0, 1))
+    H = CE.hybrid_cpu(n, dict(lam_max=lam, deg_cap=P_CAP, dense_cap=DENSE_CAP, outer=(1.0, 2.0, 3)), threads=threads)
+    G1 = O.G1_apply
+    lo, hi, D = O.outer_interval(N, H.Gh, G1, H.P, 1e-10)
+    H.lo, H.hi, H.outer_deg = lo, hi, D
+    x = pkg.phantoms.ellipse_phantom(N, seed=0)
+    b = pkg.phantoms.add_noise(A.adrt(n, x), REL_SIGMA, seed=1)
+    for _ in range(args.warmup):
+        H.apply(b)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        H.apply(b)
+    dt = (time.perf_counter() - t0) / args.steps
+    v = 1.0 / dt
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "recon/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args, 1) | {"global_batch": 1},
+            "cpu_baseline": {"value": v, "unit": "recon/s", "cores": threads, "kind": H.eng.kind,
+                             "sample": f"one N={N} sinogram per step (the batch's first), same plan"},
+            "e2e": {"value": v, "unit": "recon/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    import __graft_entry__ as ge
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    dev = torch.device("cuda", local)
+    pkg = ge.load_package()
+    C = pkg._lib
+    n, N, B = args.n, 1 << args.n, args.batch
+
+    H = pkg.FastHybridGpu(n, deg_cap=P_CAP, dense_cap=DENSE_CAP, precision="fp32", device=dev)
+    b_dev = sinograms(pkg, n, B, seed0=1000 * rank, device=dev)
+    pipe = H.pipeline(B)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    # ---- device-resident throughput
+    for _ in range(args.warmup):
+        pipe.apply(b_dev)
+    torch.cuda.synchronize()
+    timer = []
+    pipe.tables.timer = timer
+    barrier()
+    torch.cuda.synchronize()
+    l0 = C.load().adrt_launch_count()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(dev.index) as clk:
+        if args.profile_region:
+            torch.cuda.profiler.start()
+        e0.record()
+        for _ in range(args.steps):
+            pipe.apply(b_dev)
+        e1.record()
+        torch.cuda.synchronize()
+        if args.profile_region:
+            torch.cuda.profiler.stop()
+    barrier()
+    launches = (C.load().adrt_launch_count() - l0) // args.steps
+    pipe.tables.timer = None
+    ms = e0.elapsed_time(e1) / args.steps
+    ms_t = torch.tensor([ms], device=dev)
+    if world > 1:
+        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
+    ms = float(ms_t.item())
+    value = B * world / (ms * 1e-3)
+    # the G_h launches of the polynomial rows (one per outer step): mean duration and algorithmic FLOPs
+    g_ms = [a.elapsed_time(b) for a, b, ops in timer if ops == pipe.ops["G"]]
+    rows_launch_ms = float(np.mean(g_ms)) if g_ms else None
+    flops_per_launch = pipe.tables.main_level_rows(pipe.ops["G"]) * B * 8 * N
+
+    # ---- end to end through the public API with pinned host buffers
+    b_host = torch.empty(b_dev.shape, dtype=b_dev.dtype, pin_memory=True)
+    b_host.copy_(b_dev)
+    out_host = torch.empty((B, N, N), dtype=torch.float64, pin_memory=True)
+    for _ in range(2):
+        H.apply(b_host, out=out_host)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        H.apply(b_host, out=out_host)
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    barrier()
+    e2e_t = torch.tensor([e2e_s], device=dev)
+    if world > 1:
+        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
+    e2e_value = B * world / float(e2e_t.item())
+
+    if rank != 0:
+        if world > 1:
+            dist.destroy_process_group()
+        return
+
+    # ---- accuracy of this run against the FP64 CPU reference path on one image (same plan)
+    peak = fp32_peak(pkg, torch)
+    line = {"metric": METRIC, "value": value, "unit": "recon/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipse phantoms + Gaussian noise)",
+            "config": config(args, world), "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": int(b_host.numel() * 8),
+                    "d2h_bytes_per_step": int(out_host.numel() * 8)}}
+    if rows_launch_ms:
+        achieved = flops_per_launch / (rows_launch_ms * 1e-3) / 1e12
+        tr = traffic_per_launch()
+        line["roofline"] = {"bound": "fp32", "kernel": "rows_fast_kernel (G_h op list, polynomial rows)",
+                            "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved * 1e12 / peak,
+                            "peak_source": "measured in this run: FP32 FMA probe kernel",
+                            "flop_per_launch": flops_per_launch, "launch_ms": rows_launch_ms,
+                            "traffic": tr, "traffic_unit": "bytes/launch (ncu dram read+write)"}
+    if not args.no_cpu_baseline:
+        plan_kw = dict(lam_max=H.plan.lam_max, deg=H.deg, dense_cap=DENSE_CAP, outer=(H.lo, H.hi, H.outer_deg))
+        b_one = b_dev[0].cpu().numpy()
+        threads = os.cpu_count() or 1
+        t_cpu, kind = cpu_reference_time(n, plan_kw, b_one, 2, threads)
+        from oracle import cpu_engine as CE
+
+        ref = CE.hybrid_cpu(n, plan_kw, threads=threads).apply(b_one)
+        got = H.apply(b_dev[:1])[0].cpu().numpy()
+        line["rel_err_vs_fp64"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
+        line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "recon/s", "cores": threads, "kind": kind,
+                                "sample": f"one N={N} sinogram of the batch, min of 2 applies after a warm-up"}
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -59,6 +59,12 @@ int omp_max_threads(void);
 const char* adrt_last_error(void);
 /* library ABI version */
 int adrt_abi_version(void);
+/* number of CUDA kernels the library has launched so far (all threads); for launch accounting */
+long long adrt_launch_count(void);
+/* measurement utility: FP32 FMA throughput probe, blocks x threads threads each doing iters x 64 dependent-free
+ * FMAs (128 flop per thread and iteration); out: blocks*threads floats (device). Used to measure the FP32 peak
+ * that bounds the row engine. */
+int adrt_fp32_probe(int blocks, int threads, int iters, float* out, void* stream);
 
 /* ------------------------------------------------------------------ 2. device entry points */
 

@@ -32,7 +32,8 @@ def test_outer_interval_on_gpu(pkg, golden, name):
     P = cls(n, lam_max=golden[f"inv_lam_{k}"])
     lo, hi, D = golden[f"inv_outer_{k}"]
     assert np.array_equal(P.deg, golden[f"inv_deg_{k}"])
-    assert abs(P.lo - lo) < 1e-4 * lo and abs(P.hi - hi) < 1e-4 * hi
+    # eigsh tol 1e-3 from ARPACK's process-dependent start vector: agreement to a few 1e-3
+    assert abs(P.lo - lo) < 5e-3 * lo and abs(P.hi - hi) < 5e-3 * hi
     assert abs(P.outer_deg - int(D)) <= 1
 
 

@@ -145,5 +145,6 @@ def test_outer_interval_recomputed(golden):
     k = "hyb_4"
     P = O.HybridOracle(4, lam_max=golden[f"inv_lam_{k}"])
     lo, hi, D = golden[f"inv_outer_{k}"]
-    assert abs(P.lo - lo) < 1e-3 * lo and abs(P.hi - hi) < 1e-3 * hi
+    # eigsh runs at tol 1e-3 from ARPACK's process-dependent start vector: the enclosure agrees to a few 1e-3
+    assert abs(P.lo - lo) < 5e-3 * lo and abs(P.hi - hi) < 5e-3 * hi
     assert abs(P.outer_deg - D) <= 1
