@@ -24,6 +24,7 @@ void set_error(const char* fmt, ...) {
 int cuda_status(cudaError_t e, const char* where) {
     if (e == cudaSuccess) return ADRT_OK;
     set_error("%s: %s", where, cudaGetErrorString(e));
+    cudaGetLastError();  // consume a non-sticky error so that later, unrelated calls do not report it again
     return e == cudaErrorMemoryAllocation ? ADRT_ENOMEM : ADRT_ECUDA;
 }
 

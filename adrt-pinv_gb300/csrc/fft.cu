@@ -38,8 +38,14 @@ template <typename real> struct FftMax;
 template <> struct FftMax<float> { static constexpr int C = 16; };
 template <> struct FftMax<double> { static constexpr int C = 8; };
 
-template <int l> __host__ __device__ constexpr int fft_cols(int Cmax) {
-    return imax(1, imin(imin(Cmax, 1024 / FftCfg<l>::TPC), (1 << l) / 2));
+// columns per CTA: the largest power of two <= Cmax, <= 1024 / threads-per-column and <= N whose unpack tiles
+// (roots L + exchange tile L x CP + pair-(0,1) result N x CP, CP = C + 1 padding for C > 1) fit in 227 KB
+constexpr int kSmemBudget = 227 * 1024;
+__host__ __device__ constexpr int fft_pad(int c) { return c > 1 ? c + 1 : 1; }
+template <int l> __host__ __device__ constexpr int fft_cols(int Cmax, int elem_bytes) {
+    int c = imax(1, imin(imin(Cmax, 1024 / FftCfg<l>::TPC), (1 << l) / 2));
+    while (c > 1 && ((1 << l) + ((1 << l) + (1 << (l - 1))) * fft_pad(c)) * elem_bytes > kSmemBudget) c >>= 1;
+    return c;
 }
 
 // all passes of the in-place DIT transform on the registers x[] of (column c, column-thread t)
@@ -87,8 +93,8 @@ __global__ void __launch_bounds__(1024) pack_fft_kernel(int nimg, int src_kind, 
     using F = FftCfg<l>;
     using C = cplx<real>;
     constexpr int L = F::L, N = L / 2;
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
-    constexpr int CP = CB + 1;
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+    constexpr int CP = fft_pad(CB);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* roots = reinterpret_cast<C*>(smem_raw);
     C* tile = roots + L;
@@ -153,8 +159,8 @@ __global__ void __launch_bounds__(1024) ifft_unpack_kernel(int nimg, const cplx<
     using F = FftCfg<l>;
     using C = cplx<real>;
     constexpr int L = F::L, N = L / 2;
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
-    constexpr int CP = CB + 1;
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+    constexpr int CP = fft_pad(CB);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* roots = reinterpret_cast<C*>(smem_raw);
     C* tile = roots + L;          // L x CP exchange tile
@@ -197,17 +203,17 @@ __global__ void __launch_bounds__(1024) ifft_unpack_kernel(int nimg, const cplx<
 }
 
 template <typename real, int l> static size_t pack_smem() {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
-    return ((size_t)(1 << l) + (size_t)(1 << l) * (CB + 1)) * sizeof(cplx<real>);
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+    return ((size_t)(1 << l) + (size_t)(1 << l) * fft_pad(CB)) * sizeof(cplx<real>);
 }
 template <typename real, int l> static size_t unpack_smem() {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
-    return ((size_t)(1 << l) + (size_t)(1 << l) * (CB + 1) + (size_t)(1 << (l - 1)) * (CB + 1)) * sizeof(cplx<real>);
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+    return ((size_t)(1 << l) + ((size_t)(1 << l) + (size_t)(1 << (l - 1))) * fft_pad(CB)) * sizeof(cplx<real>);
 }
 
 template <typename real, int l>
 static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, cudaStream_t st) {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
     constexpr int N = 1 << (l - 1);
     const size_t smem = pack_smem<real, l>();
     auto kern = pack_fft_kernel<real, l>;
@@ -220,7 +226,7 @@ static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, v
 
 template <typename real, int l>
 static int launch_unpack(int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots, cudaStream_t st) {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C);
+    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
     constexpr int N = 1 << (l - 1);
     const size_t smem = unpack_smem<real, l>();
     auto kern = ifft_unpack_kernel<real, l>;

@@ -135,10 +135,11 @@ def test_n256_left_inverse_and_linearity(pkg, hybrid256):
 
 
 def test_batch_equals_single(pkg, hybrid256):
-    """Each result is the same alone and inside a batch (bit-identical: no cross-image arithmetic)."""
+    """Each result is the same alone and inside a batch, within 1e-6: the kernels do no cross-image arithmetic, but
+    the dense-row matrix product may sum in a different order for a different batch width."""
     n, N = 8, 256
     bs = np.stack([pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, pkg.phantoms.ellipse_phantom(N, seed=s)), 1e-3, seed=s + 100)
                    for s in range(3)])
     batch = hybrid256.apply(bs)
     for i in range(3):
-        assert np.array_equal(batch[i], hybrid256.apply(bs[i]))
+        assert rel_err(batch[i], hybrid256.apply(bs[i])) < 1e-6
