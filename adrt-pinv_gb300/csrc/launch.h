@@ -25,5 +25,9 @@ int image_outer(int dtype, int n, int nimg, const void* x, const void* xp, const
 int ensure_smem(const void* func, size_t bytes);
 int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st);
 int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st);
+int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2, const double* x,
+               const double* xp, double* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
+               const double* g1_coef, cudaStream_t st);
+int outer_step_max_n(int dtype);
 int cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, cudaStream_t st);
 }  // namespace adrt

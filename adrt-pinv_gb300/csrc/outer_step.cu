@@ -1,0 +1,210 @@
+// One image-space outer step of the inverse, fused: residual, preconditioner and outer Chebyshev update
+// (reference: fastops._outer fastops.py:247-258 with P = g1_inv / lorr_inv / identity, fasthybrid.py:101-130):
+//     s = y - (p0 + p1 + p2)                           (p* = the three partial images of G x; absent: s = y)
+//     r = P s                                          (g1: deg-step Chebyshev on the G_1 stencil over [4, 16])
+//     x_new = x + om_a r + om_1 (x - x_prev)           (x absent: x_new = a0 r)
+// One thread-block cluster per image: CTA c of the cluster keeps rows [BAND c, BAND (c+1)) of s and of the two
+// stencil iterates in shared memory for all steps; the G_1 stencil needs one row above and below the band, read
+// from the neighbouring CTAs' shared memory (distributed shared memory) after a cluster barrier per step.
+// Pair rows (2i, 2i+1) never straddle a band (BAND is even), so the i^1 neighbour is always local.
+#include <cooperative_groups.h>
+
+#include "common.cuh"
+#include "launch.h"
+
+namespace cg = cooperative_groups;
+
+namespace adrt {
+
+constexpr int OS_THREADS = 256;
+constexpr int OS_MAX_STEPS = 32;
+
+struct OuterStepArgs {
+    const double* y;
+    const void* p0;
+    const void* p1;
+    const void* p2;
+    const double* x;
+    const double* xp;
+    double* xn;
+    double om_a, om_1, a0;
+    int precond;  // 0 none, 1 g1, 2 lorr
+    int g1_deg;
+    double g1_a0;
+    double g1_om_a[OS_MAX_STEPS];
+    double g1_om_1[OS_MAX_STEPS];
+};
+
+template <typename T, int n, int BAND>
+__global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepArgs A) {
+    constexpr int N = 1 << n;
+    constexpr int CL = N / BAND;
+    constexpr int E = BAND * N;  // elements per CTA
+    cg::cluster_group cluster = cg::this_cluster();
+    const int rank = (int)cluster.block_rank();
+    const int img = blockIdx.x / CL;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* s = reinterpret_cast<T*>(smem_raw);
+    T* bufA = s + E;
+    T* bufB = bufA + E;
+    const size_t base = (size_t)img * N * N + (size_t)rank * E;
+    const T* p0 = reinterpret_cast<const T*>(A.p0);
+    const T* p1 = reinterpret_cast<const T*>(A.p1);
+    const T* p2 = reinterpret_cast<const T*>(A.p2);
+
+    // residual into shared memory
+    for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+        const size_t g = base + e;
+        const T t = p0 ? (p0[g] + p1[g]) + p2[g] : (T)0;
+        s[e] = (T)(A.y[g] - (double)t);
+    }
+    __syncthreads();
+
+    T* r = s;
+    if (A.precond == 1) {
+        // x_1 = a s ; x_{k+1} = x_k + om_a (s - G1 x_k) + om_1 (x_k - x_{k-1})   (x_0 = 0)
+        T* cur = bufA;
+        T* prv = bufB;
+        const T a0 = (T)A.g1_a0;
+        for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+            cur[e] = a0 * s[e];
+            prv[e] = (T)0;
+        }
+        cluster.sync();
+        const T* up = rank > 0 ? cluster.map_shared_rank(bufA, rank - 1) : nullptr;     // neighbour buffers, same
+        const T* dn = rank < CL - 1 ? cluster.map_shared_rank(bufA, rank + 1) : nullptr; // offsets in every CTA
+        for (int k = 1; k < A.g1_deg; ++k) {
+            const T om_a = (T)A.g1_om_a[k - 1], om_1 = (T)A.g1_om_1[k - 1];
+            const ptrdiff_t off = cur - bufA;  // the current iterate lives at the same offset in every CTA
+            const T* upc = up ? up + off : nullptr;
+            const T* dnc = dn ? dn + off : nullptr;
+            for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+                const int i = e / N, j = e - (e / N) * N;
+                const int jp = j ^ 1, ip = i ^ 1;
+                T a = (T)2 * cur[i * N + jp];
+                if (i > 0) a += cur[(i - 1) * N + jp];
+                else if (upc) a += upc[(BAND - 1) * N + jp];
+                if (i < BAND - 1) a += cur[(i + 1) * N + jp];
+                else if (dnc) a += dnc[jp];
+                T b = (T)2 * cur[ip * N + j];
+                if (j > 0) b += cur[ip * N + j - 1];
+                if (j < N - 1) b += cur[ip * N + j + 1];
+                const T g1 = ((T)8 * cur[e] + a) + b;
+                const T xv = cur[e];
+                prv[e] = xv + om_a * (s[e] - g1) + om_1 * (xv - prv[e]);
+            }
+            cluster.sync();
+            T* t = cur;
+            cur = prv;
+            prv = t;
+        }
+        r = cur;
+    } else if (A.precond == 2) {
+        // (s - Pi s)/4 + Pi s/12 with Pi the 2x2-cell mean (cells never straddle a band)
+        T* out = bufA;
+        for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+            const int i = e / N, j = e - (e / N) * N;
+            const int i0 = i & ~1, j0 = j & ~1;
+            const T m = ((s[i0 * N + j0] + s[i0 * N + j0 + 1]) + (s[(i0 + 1) * N + j0] + s[(i0 + 1) * N + j0 + 1])) / (T)4;
+            out[e] = (s[e] - m) / (T)4 + m / (T)12;
+        }
+        __syncthreads();
+        r = out;
+    }
+
+    // outer update in FP64
+    for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+        const size_t g = base + e;
+        const double rv = (double)r[e];
+        if (!A.x) {
+            A.xn[g] = A.a0 * rv;
+        } else {
+            const double xv = A.x[g];
+            const double prev = A.xp ? A.xp[g] : 0.0;
+            A.xn[g] = xv + A.om_a * rv + A.om_1 * (xv - prev);
+        }
+    }
+}
+
+template <typename T, int n>
+static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
+    constexpr int N = 1 << n;
+    constexpr int BAND = N >= 32 ? 32 : N;
+    constexpr int CL = N / BAND;
+    const size_t smem = 3 * (size_t)BAND * N * sizeof(T);
+    auto kern = outer_step_kernel<T, n, BAND>;
+    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
+    if (CL > 8) {
+        if (int rc = cuda_status(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
+                                 "outer_step cluster attribute"))
+            return rc;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nimg * CL);
+    cfg.blockDim = dim3(OS_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, A);
+    return launch_status("outer_step_kernel");
+}
+
+// largest n with a fused (cluster) outer step for element type T: the band tiles must fit 227 KB and the cluster
+// at most 16 CTAs (non-portable size above 8)
+int outer_step_max_n(int dtype) { return dtype == ADRT_F32 ? 9 : 8; }
+
+int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2, const double* x,
+               const double* xp, double* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
+               const double* g1_coef, cudaStream_t st) {
+    if ((dtype != ADRT_F32 && dtype != ADRT_F64) || n < 1 || n > outer_step_max_n(dtype) || nimg < 0 || precond < 0 ||
+        precond > 2 || (precond == 1 && (g1_deg < 1 || g1_deg > OS_MAX_STEPS || !g1_coef)) || (p0 && (!p1 || !p2))) {
+        set_error("outer_step: bad arguments (dtype=%d n=%d precond=%d deg=%d)", dtype, n, precond, g1_deg);
+        return ADRT_EINVAL;
+    }
+    if (!nimg) return ADRT_OK;
+    if (!y || !xn) { set_error("outer_step: null pointer"); return ADRT_EINVAL; }
+    OuterStepArgs A = {};
+    A.y = y; A.p0 = p0; A.p1 = p1; A.p2 = p2; A.x = x; A.xp = xp; A.xn = xn;
+    A.om_a = om_a; A.om_1 = om_1; A.a0 = a0; A.precond = precond; A.g1_deg = g1_deg;
+    if (precond == 1) {
+        A.g1_a0 = g1_coef[0];
+        for (int k = 1; k < g1_deg; ++k) {
+            A.g1_om_a[k - 1] = g1_coef[2 * k - 1];
+            A.g1_om_1[k - 1] = g1_coef[2 * k];
+        }
+    }
+    if (dtype == ADRT_F32) {
+        switch (n) {
+            case 1: return launch_os<float, 1>(A, nimg, st);
+            case 2: return launch_os<float, 2>(A, nimg, st);
+            case 3: return launch_os<float, 3>(A, nimg, st);
+            case 4: return launch_os<float, 4>(A, nimg, st);
+            case 5: return launch_os<float, 5>(A, nimg, st);
+            case 6: return launch_os<float, 6>(A, nimg, st);
+            case 7: return launch_os<float, 7>(A, nimg, st);
+            case 8: return launch_os<float, 8>(A, nimg, st);
+            case 9: return launch_os<float, 9>(A, nimg, st);
+        }
+    } else {
+        switch (n) {
+            case 1: return launch_os<double, 1>(A, nimg, st);
+            case 2: return launch_os<double, 2>(A, nimg, st);
+            case 3: return launch_os<double, 3>(A, nimg, st);
+            case 4: return launch_os<double, 4>(A, nimg, st);
+            case 5: return launch_os<double, 5>(A, nimg, st);
+            case 6: return launch_os<double, 6>(A, nimg, st);
+            case 7: return launch_os<double, 7>(A, nimg, st);
+            case 8: return launch_os<double, 8>(A, nimg, st);
+        }
+    }
+    set_error("outer_step: n=%d unsupported", n);
+    return ADRT_EUNSUPPORTED;
+}
+
+}  // namespace adrt

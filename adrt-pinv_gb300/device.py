@@ -247,6 +247,23 @@ class Pipeline:
             prev, cur = cur, nxt
         return bufs[cur]
 
+    def fused_outer_ok(self):
+        return self.plan.n <= C.load().adrt_outer_step_max_n(C.dtype_code(self.stencil_real))
+
+    def fused_outer_step(self, y, with_parts, x, x_prev, x_new, om_a, om_1, a0):
+        """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step)."""
+        p = self.plan
+        pc = {"none": 0, "g1": 1, "lorr": 2}[p.precond] if p.method == "hybrid" else 0
+        if pc == 1:
+            ga, _, gsteps = outer_coeffs(4.0, 16.0, p.g1_deg)
+            coef = np.array([ga] + [v for st in gsteps for v in st], dtype=np.float64)
+        else:
+            coef = np.zeros(1)
+        parts = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
+        C.call("adrt_outer_step", C.dtype_code(self.stencil_real), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
+               C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
+               p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.stream_handle())
+
     def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0):
         C.call("adrt_outer_update", C.dtype_code(x_new.dtype), self.plan.n, self.B, C.ptr(x), C.ptr(x_prev), C.ptr(r),
                C.dtype_code(r.dtype), C.ptr(x_new), om_a, om_1, a0, C.stream_handle())
@@ -269,8 +286,11 @@ class Pipeline:
         a, c, steps = outer_coeffs(p.lo, p.hi, p.outer_deg)
         y = self.backproject_into(b, self.y)
         hybrid = p.method == "hybrid"
+        fused = self.fused_outer_ok() and self.parts.dtype == self.stencil_real
         x, xp = self.xs[0], None
-        if hybrid:
+        if fused:
+            self.fused_outer_step(y, False, None, None, x, 0.0, 0.0, a)
+        elif hybrid:
             r = self.precond(self.resid(y, with_parts=False))
             self.outer_step(None, None, r, x, 0.0, 0.0, a)
         else:
@@ -278,10 +298,13 @@ class Pipeline:
         free = [self.xs[1], self.xs[2]]
         for om_a, om_1 in steps:
             self.G(x)
-            s = self.resid(y)
-            r = self.precond(s) if hybrid else s
             xn = free.pop(0)
-            self.outer_step(x, xp, r, xn, om_a, om_1, 0.0)
+            if fused:
+                self.fused_outer_step(y, True, x, xp, xn, om_a, om_1, 0.0)
+            else:
+                s = self.resid(y)
+                r = self.precond(s) if hybrid else s
+                self.outer_step(x, xp, r, xn, om_a, om_1, 0.0)
             if xp is not None:
                 free.append(xp)
             xp, x = x, xn

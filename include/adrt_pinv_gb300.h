@@ -140,6 +140,17 @@ int adrt_outer_update(int dtype, int n, int nimg, const void* x, const void* x_p
 int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const void* p2, void* out, int out_dtype,
               void* stream);
 
+/* One fused outer step (fastops._outer, fastops.py:247-258, with P of fasthybrid.py:101-130):
+ *   s = y - (p0 + p1 + p2) (parts in dtype, all NULL: s = y);  r = P s  (precond 0: identity, 1: g1_inv with
+ *   g1_deg steps, 2: lorr_inv);  x_new = x + om_a r + om_1 (x - x_prev)  (x == NULL: x_new = a0 r; x_prev NULL: 0).
+ * y, x, x_prev, x_new are FP64; s and the stencil iterates are dtype. One thread-block cluster per image keeps the
+ * image in shared memory for every stencil step. g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
+ * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). Supported: n <= adrt_outer_step_max_n(dtype). */
+int adrt_outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2,
+                    const double* x, const double* x_prev, double* x_new, double om_a, double om_1, double a0,
+                    int precond, int g1_deg, const double* g1_coef, void* stream);
+int adrt_outer_step_max_n(int dtype);
+
 /* Spatial ADRT in the reference's sinogram layout (adrtcore.py:122-137), nimg images, exact for integer dtypes
  * (ADRT_I32, ADRT_I64; sums only), FP32 / FP64 otherwise. scratch: 2 * nimg * 4 * (2N-1) * N elements of dtype.
  * forward: x (nimg x N x N) -> b (nimg x 4 x (2N-1) x N); transpose: b -> x. */

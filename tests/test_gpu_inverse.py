@@ -143,3 +143,35 @@ def test_batch_equals_single(pkg, hybrid256):
     batch = hybrid256.apply(bs)
     for i in range(3):
         assert rel_err(batch[i], hybrid256.apply(bs[i])) < 1e-6
+
+
+@pytest.mark.parametrize("prec", ["fp32", "fp64"])
+@pytest.mark.parametrize("n,precond", [(5, "g1"), (8, "g1"), (8, "lorr"), (9, "g1"), (6, "none")])
+def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond):
+    """adrt_outer_step (residual + P + outer update, one clustered kernel) equals resid / g1 steps / outer kernels."""
+    import torch
+
+    if prec == "fp64" and n > 8:
+        pytest.skip("FP64 fused step covers n <= 8")
+    N = 1 << n
+    method = "lp" if precond == "none" else "hybrid"
+    plan = pkg.Plan(method, n, np.full(2 * N, 4.0), precond="g1" if precond == "none" else precond, outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, 3, prec)
+    assert pipe.fused_outer_ok()
+    g = torch.Generator(device="cuda").manual_seed(n)
+    y = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
+    pipe.parts.normal_(generator=g)
+    x = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
+    xp = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
+    out_f = torch.empty_like(x)
+    out_s = torch.empty_like(x)
+    pipe.fused_outer_step(y, True, x, xp, out_f, 0.7, 0.3, 0.0)
+    s = pipe.resid(y)
+    r = pipe.precond(s) if method == "hybrid" else s
+    pipe.outer_step(x, xp, r, out_s, 0.7, 0.3, 0.0)
+    tol = 1e-6 if prec == "fp32" else 1e-13
+    assert (out_f - out_s).abs().max().item() / out_s.abs().max().item() < tol
+    pipe.fused_outer_step(y, False, None, None, out_f, 0.0, 0.0, 0.25)
+    r = pipe.precond(pipe.resid(y, with_parts=False)) if method == "hybrid" else y
+    pipe.outer_step(None, None, r, out_s, 0.0, 0.0, 0.25)
+    assert (out_f - out_s).abs().max().item() / out_s.abs().max().item() < tol
