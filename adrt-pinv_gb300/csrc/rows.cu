@@ -263,7 +263,7 @@ __global__ void __launch_bounds__(THREADS, 1)
                     const real a = cf[0];
                     C zp[R];
 #pragma unroll
-                    for (int j = 0; j < R; j += 2) st2(ybuf + j + R * u, v[j], v[j + 1]);
+                    for (int j = 0; j < R; j += 2) st2(ybuf + F::phys(j + R * u), v[j], v[j + 1]);
 #pragma unroll
                     for (int j = 0; j < R; ++j) {
                         v[j] = cscale(a, v[j]);
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(THREADS, 1)
 #pragma unroll
                         for (int j = 0; j < R; j += 2) {
                             C y0, y1;
-                            ld2(ybuf + j + R * u, y0, y1);
+                            ld2(ybuf + F::phys(j + R * u), y0, y1);
                             w[j] = csub(y0, w[j]);
                             w[j + 1] = csub(y1, w[j + 1]);
                         }
@@ -330,6 +330,174 @@ __global__ void __launch_bounds__(THREADS, 1)
             } else {
 #pragma unroll
                 for (int j = 0; j < R; j += 2) st2(ptr + j + R * u, v[j], v[j + 1]);
+            }
+        }
+        if (last) break;
+    }
+}
+
+// ------------------------------------------------------------------ compile-time programs (the hot op lists)
+// The four op lists of the packed inverses (fastops.py:277-285, 325-335) with their level ranges fixed at compile
+// time: no op interpreter, no runtime level checks, one Gram body in the code (the trailing M of G_h / frame
+// reuses the loop body), the first forward level out of place (no copy of z), and the recurrence in momentum form
+//     r = y - M z - tau z ;  d = om a r + (om - 1) d ;  z = z + d          (d = z_j - z_{j-1}; z_1 = d_1 = a y)
+// which equals z_{j+1} = z_j + om a r + (om - 1)(z_j - z_{j-1}) (cpp/oblique.cpp:93-97) without register rotation.
+constexpr int FAST_THREADS = 256;
+enum { PROG_GH_HYB = 1, PROG_BP_HYB = 2, PROG_FRAME_LP = 3, PROG_BP_LP = 4 };
+
+template <typename C, int n> struct CtLanes {
+    using F = FastCfg<n>;
+    using Ln = Lanes<C, n>;
+    static constexpr int r = F::r, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
+    // forward levels LO..HI; level LO reads src and writes dst, the rest run in place on dst (A layout in and out)
+    template <int LO, int HI>
+    __device__ __forceinline__ static void fwd_oop(const C (&src)[R], C (&dst)[R], const C (&tA)[R / 2 + 1],
+                                                   const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], C* buf, int u,
+                                                   unsigned gm) {
+#pragma unroll
+        for (int b = 0; b < r; ++b) {
+            if (b + 1 >= LO && b + 1 <= HI) {
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    if (j & (1 << b)) continue;
+                    const int t = brev(j & ((1 << b) - 1), b);
+                    const C f0 = (b + 1 == LO) ? src[j] : dst[j];
+                    const C f1 = (b + 1 == LO) ? src[j | (1 << b)] : dst[j | (1 << b)];
+                    dst[j] = cfma(tA[t], f1, f0);
+                    dst[j | (1 << b)] = cfma(tA[t + 1], f1, f0);
+                }
+            }
+        }
+        if (HI > r) {
+            Ln::toB(dst, buf, u, gm);
+            Ln::fwdB(dst, t0, t1, LO, HI);
+        }
+    }
+    // Gram M = B^* B over LO..HI: src (A layout) -> dst (A layout)
+    template <int LO, int HI>
+    __device__ __forceinline__ static void gram_oop(const C (&src)[R], C (&dst)[R], const C (&tA)[R / 2 + 1],
+                                                    const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], C* buf,
+                                                    int u, unsigned gm) {
+        fwd_oop<LO, HI>(src, dst, tA, t0, t1, buf, u, gm);
+        if (HI > r) {
+            Ln::adjB(dst, t0, t1, LO, HI);
+            Ln::toA(dst, buf, u, gm);
+        }
+        Ln::adjA(dst, tA, LO, HI);
+    }
+};
+
+template <typename real, int n, int THREADS, int PROG>
+__global__ void __launch_bounds__(THREADS, 1)
+    rows_prog_kernel(const adrt_row_job J, const TwSrc<real> tw, const int total) {
+    using C = cplx<real>;
+    using F = FastCfg<n>;
+    using Ln = Lanes<C, n>;
+    using Ct = CtLanes<C, n>;
+    constexpr int N = F::N, r = F::r, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
+    constexpr int GPW = 32 / T;
+    constexpr bool HYB = (PROG == PROG_GH_HYB || PROG == PROG_BP_HYB);
+    constexpr int LO = HYB ? 2 : 1;  // filter levels LO..n
+    constexpr bool BP = (PROG == PROG_BP_HYB || PROG == PROG_BP_LP);
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int giw = lane / T;
+    const int u = lane & (T - 1);
+    C* buf = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / T) * (F::BUF + F::N);
+    C* ybuf = buf + F::BUF;
+    const unsigned gm = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (giw * T));
+    C* X = reinterpret_cast<C*>(J.X);
+    const real tau = (real)J.tau;
+    const real* coefs = reinterpret_cast<const real*>(J.coef);
+
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(J.counter, GPW);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= total) break;
+        const bool last = base + GPW >= total;
+        const int item = base + giw;
+        if (item < total) {
+            const int sel = item / J.nimg;
+            const int img = item - sel * J.nimg;
+            const int row = J.rows ? J.rows[sel] : sel;
+            const int k = row % J.freq_mod;
+            const int key = tw.roots ? k : row;
+            C* ptr = X + (size_t)img * J.img_stride + (size_t)row * N;
+            const real* cf = coefs + (size_t)k * J.coef_stride;
+            const int d = J.deg[k];
+            const real a = cf[0];
+
+            C tA[R / 2 + 1];
+#pragma unroll
+            for (int t = 0; t <= R / 2; ++t) tA[t] = tw.get(key, t);
+            C t0[NB ? NB : 1], t1[NB ? NB : 1];
+            if (NB) {
+                const int U = tb ? (int)(__brev((unsigned)u) >> (32 - tb)) : 0;
+#pragma unroll
+                for (int b = r; b < n; ++b) {
+                    const int jb = b - tb;
+#pragma unroll
+                    for (int vv = 0; vv < (1 << jb); ++vv) {
+                        const int t = (U << jb) + brev(vv, jb);
+                        t0[F::offB(b) + vv] = tw.get(key, t);
+                        t1[F::offB(b) + vv] = tw.get(key, t + 1);
+                    }
+                }
+            }
+
+            C v[R], w[R], dl[R];
+            if (BP) {
+                // the back-projections start with the adjoint levels LO..n on rows in natural (slope) order
+#pragma unroll
+                for (int j = 0; j < R; ++j) v[j] = ptr[bfly_perm(j + R * u, n)];
+                Ln::adj(v, tA, t0, t1, LO, n, buf, u, gm);
+            } else {
+#pragma unroll
+                for (int j = 0; j < R; j += 2) ld2(ptr + j + R * u, v[j], v[j + 1]);
+                if (PROG == PROG_GH_HYB) Ln::fwdA(v, tA, 1, 1);  // B_1
+            }
+            // filter input y -> shared memory; z_1 = d_1 = a y
+#pragma unroll
+            for (int j = 0; j < R; j += 2) st2(ybuf + F::phys(j + R * u), v[j], v[j + 1]);
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                v[j] = cscale(a, v[j]);
+                dl[j] = v[j];
+            }
+            // G_h and the frame end with M applied to z_d: one more pass of the loop body without the update
+            const int steps = BP ? d - 1 : d;
+            real om_a = d > 1 ? cf[2] : (real)0, om_1 = d > 1 ? cf[3] : (real)0;  // step 1
+            for (int s = 1; s <= steps; ++s) {
+                const real na = (s + 1 < d) ? cf[3 * s + 2] : (real)0, n1 = (s + 1 < d) ? cf[3 * s + 3] : (real)0;
+                Ct::template gram_oop<LO, n>(v, w, tA, t0, t1, buf, u, gm);
+                if (s == d) break;  // w = M z_d
+#pragma unroll
+                for (int j = 0; j < R; j += 2) {
+                    C y0, y1;
+                    ld2(ybuf + F::phys(j + R * u), y0, y1);
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const C yy = h ? y1 : y0;
+                        C rr = csub(yy, w[j + h]);
+                        rr.x = fma(-tau, v[j + h].x, rr.x);
+                        rr.y = fma(-tau, v[j + h].y, rr.y);
+                        dl[j + h].x = fma(om_1, dl[j + h].x, om_a * rr.x);
+                        dl[j + h].y = fma(om_1, dl[j + h].y, om_a * rr.y);
+                        v[j + h] = cadd(v[j + h], dl[j + h]);
+                    }
+                }
+                om_a = na;
+                om_1 = n1;
+            }
+            if (BP) {
+                if (PROG == PROG_BP_HYB) Ln::adjA(v, tA, 1, 1);  // B_1^*
+#pragma unroll
+                for (int j = 0; j < R; j += 2) st2(ptr + j + R * u, v[j], v[j + 1]);
+            } else {
+                if (PROG == PROG_GH_HYB) Ln::adjA(w, tA, 1, 1);  // B_1^*
+#pragma unroll
+                for (int j = 0; j < R; j += 2) st2(ptr + j + R * u, w[j], w[j + 1]);
             }
         }
         if (last) break;
@@ -506,7 +674,6 @@ static int num_sms() {
 
 int device_sm_count() { return num_sms(); }
 
-constexpr int FAST_THREADS = 256;
 
 template <typename real, int n>
 static int launch_fast(const adrt_row_job& J, const TwSrc<real>& tw, int total, int iters, double safety, double* pout,
@@ -552,6 +719,37 @@ static bool fast_ok(const adrt_row_job& J) {
     return true;
 }
 
+template <typename real, int n>
+static int launch_prog(const adrt_row_job& J, const TwSrc<real>& tw, int total, int prog, cudaStream_t st) {
+    using F = FastCfg<n>;
+    const size_t smem = (size_t)(FAST_THREADS / F::T) * (F::BUF + F::N) * sizeof(cplx<real>);
+    void (*kern)(const adrt_row_job, const TwSrc<real>, const int) = nullptr;
+    switch (prog) {
+        case PROG_GH_HYB: kern = rows_prog_kernel<real, n, FAST_THREADS, PROG_GH_HYB>; break;
+        case PROG_BP_HYB: kern = rows_prog_kernel<real, n, FAST_THREADS, PROG_BP_HYB>; break;
+        case PROG_FRAME_LP: kern = rows_prog_kernel<real, n, FAST_THREADS, PROG_FRAME_LP>; break;
+        default: kern = rows_prog_kernel<real, n, FAST_THREADS, PROG_BP_LP>; break;
+    }
+    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
+    const int grid = J.grid > 0 ? J.grid : num_sms();
+    kern<<<grid, FAST_THREADS, smem, st>>>(J, tw, total);
+    return launch_status("rows_prog_kernel");
+}
+
+// the op lists of the packed inverses, recognised for the compile-time kernels (hybrid needs n >= 2)
+static int match_prog(const adrt_row_job& J) {
+    const int n = J.n;
+    auto is = [&](int o, int op, int lo, int hi) { return J.op[o] == op && J.lo[o] == lo && J.hi[o] == hi; };
+    if (n >= 2 && J.nops == 4 && is(0, ADRT_OP_B, 1, 1) && is(1, ADRT_OP_P, 2, n) && is(2, ADRT_OP_M, 2, n) &&
+        is(3, ADRT_OP_BT, 1, 1))
+        return PROG_GH_HYB;
+    if (n >= 2 && J.nops == 3 && is(0, ADRT_OP_BT, 2, n) && is(1, ADRT_OP_P, 2, n) && is(2, ADRT_OP_BT, 1, 1))
+        return PROG_BP_HYB;
+    if (J.nops == 2 && is(0, ADRT_OP_P, 1, n) && is(1, ADRT_OP_M, 1, n)) return PROG_FRAME_LP;
+    if (J.nops == 2 && is(0, ADRT_OP_BT, 1, n) && is(1, ADRT_OP_P, 1, n)) return PROG_BP_LP;
+    return 0;
+}
+
 template <typename real>
 static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double* pout, cudaStream_t st) {
     TwSrc<real> tw;
@@ -566,6 +764,19 @@ static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double
         return ADRT_EINVAL;
     }
     const int total = (int)total_l;
+    const int prog = (!pout && fast_ok(J)) ? match_prog(J) : 0;
+    if (prog) {
+        switch (J.n) {
+            case 1: return launch_prog<real, 1>(J, tw, total, prog, st);
+            case 2: return launch_prog<real, 2>(J, tw, total, prog, st);
+            case 3: return launch_prog<real, 3>(J, tw, total, prog, st);
+            case 4: return launch_prog<real, 4>(J, tw, total, prog, st);
+            case 5: return launch_prog<real, 5>(J, tw, total, prog, st);
+            case 6: return launch_prog<real, 6>(J, tw, total, prog, st);
+            case 7: return launch_prog<real, 7>(J, tw, total, prog, st);
+            case 8: return launch_prog<real, 8>(J, tw, total, prog, st);
+        }
+    }
     if (fast_ok(J)) {
         switch (J.n) {
             case 1: return launch_fast<real, 1>(J, tw, total, iters, safety, pout, st);
