@@ -55,6 +55,16 @@ int cert_rowsum(int n, int K, const double* omega, int m_lo, double* out, int nt
 /* cpp/oblique.cpp:132 omp_max_threads: here the number of SMs of the current device (the row parallelism). */
 int omp_max_threads(void);
 
+/* bfly_rows on DEVICE pointers for callers that cannot allocate device memory (a process that gives all GPU memory
+ * to its own pool, code that must not let cudaMalloc/cudaFree synchronize the device, threads that may not enter the
+ * CUDA allocator). No counterpart in the reference. Same arguments and result as bfly_rows, with z (K complex128)
+ * and X (K x N complex128, transformed in place) in device memory, 16-byte aligned, ordered on `stream`. It calls no
+ * allocator: its scratch (twiddle table + work counter) is a fixed 4 MiB device array held by every GPU that loads
+ * the library until exit; calls needing more than 256 + 16 K (N/2 + 1) bytes of it are rejected with ADRT_EINVAL.
+ * The first call on a device looks the array's address up (cudaGetSymbolAddress): make it before any stream capture.
+ * All calls share the array: calls that overlap on the GPU race on it. */
+int adrt_bfly_rows_noalloc(int n, int K, const double* z, double* X, int m_lo, int m_hi, int transpose, void* stream);
+
 /* message of the last error on the calling thread ("" if none) */
 const char* adrt_last_error(void);
 /* library ABI version */
