@@ -126,137 +126,6 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     }
 }
 
-// Register-resident variant for 64 <= N <= 256 (FP32): thread j of a CTA owns column j of the CTA's 32-row band
-// in registers (s, current and previous iterate). Per stencil step the current band is written to one of two shared
-// buffers (alternating, so a neighbour still reading the previous step's halo never sees it overwritten), a cluster
-// barrier publishes it, and the stencil reads: x(i, j^1) by warp shuffle, x(i^1, j+-1) from the local buffer,
-// x(-1, j^1) / x(32, j^1) from the neighbouring CTAs' buffers (distributed shared memory).
-constexpr int RB = 32;  // band rows held in registers
-
-template <int n>
-__global__ void __launch_bounds__(1 << n) outer_step_reg_kernel(const OuterStepArgs A) {
-    using T = float;
-    constexpr int N = 1 << n;
-    constexpr int CL = N / RB;
-    cg::cluster_group cluster = cg::this_cluster();
-    const int rank = (int)cluster.block_rank();
-    const int img = blockIdx.x / CL;
-    const int j = threadIdx.x;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* xs = reinterpret_cast<T*>(smem_raw);  // [2][RB][N]
-    const size_t base = (size_t)img * N * N + (size_t)rank * RB * N + j;
-    const T* p0 = reinterpret_cast<const T*>(A.p0);
-    const T* p1 = reinterpret_cast<const T*>(A.p1);
-    const T* p2 = reinterpret_cast<const T*>(A.p2);
-
-    T s[RB], cur[RB], prv[RB];
-#pragma unroll
-    for (int i = 0; i < RB; ++i) {
-        const size_t g = base + (size_t)i * N;
-        const T t = p0 ? (p0[g] + p1[g]) + p2[g] : (T)0;
-        s[i] = (T)(A.y[g] - (double)t);
-    }
-    if (A.precond == 1) {
-        const T a0 = (T)A.g1_a0;
-#pragma unroll
-        for (int i = 0; i < RB; ++i) {
-            cur[i] = a0 * s[i];
-            prv[i] = (T)0;
-        }
-        const T* up[2] = {nullptr, nullptr};
-        const T* dn[2] = {nullptr, nullptr};
-        if (rank > 0) {
-            up[0] = cluster.map_shared_rank(xs, rank - 1);
-            up[1] = up[0] + RB * N;
-        }
-        if (rank < CL - 1) {
-            dn[0] = cluster.map_shared_rank(xs, rank + 1);
-            dn[1] = dn[0] + RB * N;
-        }
-        const int jp = j ^ 1;
-        for (int k = 1; k < A.g1_deg; ++k) {
-            const int b = k & 1;
-            T* mine = xs + b * RB * N;
-#pragma unroll
-            for (int i = 0; i < RB; ++i) mine[i * N + j] = cur[i];
-            cluster.sync();
-            const T om_a = (T)A.g1_om_a[k - 1], om_1 = (T)A.g1_om_1[k - 1];
-            const T hu = up[b] ? up[b][(RB - 1) * N + jp] : (T)0;  // x(-1, j^1) from the band above
-            const T hd = dn[b] ? dn[b][jp] : (T)0;                 // x(RB, j^1) from the band below
-            T xo[RB];
-#pragma unroll
-            for (int i = 0; i < RB; ++i) xo[i] = __shfl_xor_sync(0xffffffffu, cur[i], 1);  // x(i, j^1)
-#pragma unroll
-            for (int i = 0; i < RB; ++i) {
-                const int ip = i ^ 1;
-                T a = (T)2 * xo[i];
-                a += (i > 0) ? xo[i - 1] : hu;
-                a += (i < RB - 1) ? xo[i + 1] : hd;
-                T bb = (T)2 * cur[ip];
-                if (j > 0) bb += mine[ip * N + j - 1];
-                if (j < N - 1) bb += mine[ip * N + j + 1];
-                const T g1 = ((T)8 * cur[i] + a) + bb;
-                const T nx = cur[i] + om_a * (s[i] - g1) + om_1 * (cur[i] - prv[i]);
-                prv[i] = cur[i];
-                cur[i] = nx;
-            }
-        }
-        cluster.sync();  // no CTA leaves while a neighbour may still read its buffers
-    } else if (A.precond == 2) {
-        // 2x2-cell means: the row partner is in registers, the column partner one lane away
-#pragma unroll
-        for (int i = 0; i < RB; i += 2) {
-            const T c0 = s[i] + s[i + 1];
-            const T m = (c0 + __shfl_xor_sync(0xffffffffu, c0, 1)) / (T)4;
-            cur[i] = (s[i] - m) / (T)4 + m / (T)12;
-            cur[i + 1] = (s[i + 1] - m) / (T)4 + m / (T)12;
-        }
-    } else {
-#pragma unroll
-        for (int i = 0; i < RB; ++i) cur[i] = s[i];
-    }
-#pragma unroll
-    for (int i = 0; i < RB; ++i) {
-        const size_t g = base + (size_t)i * N;
-        const double rv = (double)cur[i];
-        if (!A.x) {
-            A.xn[g] = A.a0 * rv;
-        } else {
-            const double xv = A.x[g];
-            const double prev = A.xp ? A.xp[g] : 0.0;
-            A.xn[g] = xv + A.om_a * rv + A.om_1 * (xv - prev);
-        }
-    }
-}
-
-template <int n>
-static int launch_os_reg(const OuterStepArgs& A, int nimg, cudaStream_t st) {
-    constexpr int N = 1 << n;
-    constexpr int CL = N / RB;
-    const size_t smem = 2 * (size_t)RB * N * sizeof(float);
-    auto kern = outer_step_reg_kernel<n>;
-    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
-    if (CL > 8) {
-        if (int rc = cuda_status(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
-                                 "outer_step cluster attribute"))
-            return rc;
-    }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3(nimg * CL);
-    cfg.blockDim = dim3(N);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeClusterDimension;
-    attr[0].val.clusterDim.x = CL;
-    attr[0].val.clusterDim.y = 1;
-    attr[0].val.clusterDim.z = 1;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, A);
-    return launch_status("outer_step_reg_kernel");
-}
-
 template <typename T, int n>
 static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     constexpr int N = 1 << n;
@@ -311,11 +180,6 @@ int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, cons
         }
     }
     if (dtype == ADRT_F32) {
-        switch (n) {
-            case 6: return launch_os_reg<6>(A, nimg, st);
-            case 7: return launch_os_reg<7>(A, nimg, st);
-            case 8: return launch_os_reg<8>(A, nimg, st);
-        }
         switch (n) {
             case 1: return launch_os<float, 1>(A, nimg, st);
             case 2: return launch_os<float, 2>(A, nimg, st);
