@@ -16,7 +16,7 @@ namespace cg = cooperative_groups;
 
 namespace adrt {
 
-constexpr int OS_THREADS = 256;
+constexpr int OS_THREADS = 512;
 constexpr int OS_MAX_STEPS = 32;
 
 struct OuterStepArgs {
@@ -73,25 +73,43 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
         cluster.sync();
         const T* up = rank > 0 ? cluster.map_shared_rank(bufA, rank - 1) : nullptr;     // neighbour buffers, same
         const T* dn = rank < CL - 1 ? cluster.map_shared_rank(bufA, rank + 1) : nullptr; // offsets in every CTA
+        // thread -> (column j, group of row pairs); a row pair (2m, 2m+1) is updated together: the transposed
+        // stencil term of each row reads the other row of the pair, the K term the rows above and below
+        constexpr int CPP = N < OS_THREADS ? N : OS_THREADS;  // columns covered per pass of the CTA
+        constexpr int RG = OS_THREADS / CPP;                  // row-pair groups
+        const int j0 = threadIdx.x % CPP, grp = threadIdx.x / CPP;
         for (int k = 1; k < A.g1_deg; ++k) {
             const T om_a = (T)A.g1_om_a[k - 1], om_1 = (T)A.g1_om_1[k - 1];
             const ptrdiff_t off = cur - bufA;  // the current iterate lives at the same offset in every CTA
             const T* upc = up ? up + off : nullptr;
             const T* dnc = dn ? dn + off : nullptr;
-            for (int e = threadIdx.x; e < E; e += OS_THREADS) {
-                const int i = e / N, j = e - (e / N) * N;
-                const int jp = j ^ 1, ip = i ^ 1;
-                T a = (T)2 * cur[i * N + jp];
-                if (i > 0) a += cur[(i - 1) * N + jp];
-                else if (upc) a += upc[(BAND - 1) * N + jp];
-                if (i < BAND - 1) a += cur[(i + 1) * N + jp];
-                else if (dnc) a += dnc[jp];
-                T b = (T)2 * cur[ip * N + j];
-                if (j > 0) b += cur[ip * N + j - 1];
-                if (j < N - 1) b += cur[ip * N + j + 1];
-                const T g1 = ((T)8 * cur[e] + a) + b;
-                const T xv = cur[e];
-                prv[e] = xv + om_a * (s[e] - g1) + om_1 * (xv - prv[e]);
+            for (int j = j0; j < N; j += CPP) {
+                const int jp = j ^ 1;
+                const bool hl = j > 0, hr = j < N - 1;
+#pragma unroll 4
+                for (int m = grp; m < BAND / 2; m += RG) {
+                    const int r0 = 2 * m, r1 = r0 + 1;
+                    const T c0 = cur[r0 * N + j], c1 = cur[r1 * N + j];
+                    const T q0 = cur[r0 * N + jp], q1 = cur[r1 * N + jp];
+                    const T qm = r0 > 0 ? cur[(r0 - 1) * N + jp] : (upc ? upc[(BAND - 1) * N + jp] : (T)0);
+                    const T qp = r1 < BAND - 1 ? cur[(r1 + 1) * N + jp] : (dnc ? dnc[jp] : (T)0);
+                    T b0 = (T)2 * c1, b1 = (T)2 * c0;
+                    if (hl) {
+                        b0 += cur[r1 * N + j - 1];
+                        b1 += cur[r0 * N + j - 1];
+                    }
+                    if (hr) {
+                        b0 += cur[r1 * N + j + 1];
+                        b1 += cur[r0 * N + j + 1];
+                    }
+                    const T a0 = ((T)2 * q0 + qm) + q1;  // K along rows (i-1 term first, then i+1)
+                    const T a1 = ((T)2 * q1 + q0) + qp;
+                    const T g0 = ((T)8 * c0 + a0) + b0;
+                    const T g1 = ((T)8 * c1 + a1) + b1;
+                    const int e0 = r0 * N + j, e1 = r1 * N + j;
+                    prv[e0] = c0 + om_a * (s[e0] - g0) + om_1 * (c0 - prv[e0]);
+                    prv[e1] = c1 + om_a * (s[e1] - g1) + om_1 * (c1 - prv[e1]);
+                }
             }
             cluster.sync();
             T* t = cur;
