@@ -280,6 +280,11 @@ int adrt_outer_step(int dtype, int n, int nimg, const double* y, const void* p0,
 
 int adrt_outer_step_max_n(int dtype) { return outer_step_max_n(dtype); }
 
+int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
+                    long long img_stride, void* Zd, int32_t* err, int use_tc, void* stream) {
+    return dense_rows(dtype, n, nimg, nrows, rows, W, Y, img_stride, Zd, err, use_tc, as_stream(stream));
+}
+
 int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scratch, void* stream) {
     return adrt_fwd(dtype, n, nimg, x, b, scratch, as_stream(stream));
 }

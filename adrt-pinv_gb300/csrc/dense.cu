@@ -1,0 +1,309 @@
+// Dense low-frequency rows: for every dense row r of the packed rows and every image b,
+//     Z[r, b] = W_r Y[b, row_r]        (W_r: N x N complex, the row's exact operator; reference: fastops.py:28-40,
+//                                       100-117, with the butterflies around the filter folded into W_r on the host)
+// computed out of place into Zd (nrows x nimg x N) and scattered back into Y.
+//
+// Tensor-core kernel (N >= 64, FP32 data): the complex product in real form,
+//     [Re z; Im z] (2N x B) = [[Re W, -Im W], [Im W, Re W]] (2N x 2N) . [Re y; Im y] (2N x B),
+// on tcgen05.mma kind::tf32 with the 3xTF32 split (a = a_hi + a_lo, products hi.hi + hi.lo + lo.hi, FP32 accumulation
+// in tensor memory): about FP32 accuracy, which these rows need (they carry most of the image energy). One CTA per
+// (dense row, 128 real output rows, batch tile); K in chunks of 32: the threads convert and store A / X tiles into
+// shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core matrices, 128 B apart along K,
+// 1024 B apart along M / N), one thread issues 12 MMAs per chunk and commits them to an mbarrier that every thread
+// waits on (bounded) before the tiles are overwritten. The tensor-memory accumulator holds one chunk only: after every
+// chunk the four warps read its 128 lanes (tcgen05.ld) and add them into FP32 registers, because accumulating all of K
+// in tensor memory measured 2e-6..7e-6 relative error growing with K (truncating accumulation), against 1e-7 here.
+//
+// CUDA-core kernel: the same product for any N and for FP64.
+#include "common.cuh"
+#include "launch.h"
+
+namespace adrt {
+
+// ------------------------------------------------------------------ scatter and CUDA-core product
+template <typename C>
+__global__ void dense_scatter_kernel(int N, int nimg, int nrows, const int* __restrict__ rows, const C* __restrict__ Zd,
+                                     C* __restrict__ Y, long long img_stride) {
+    const long long total = (long long)nrows * nimg * N;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long rb = e / N;
+        const int o = (int)(e - rb * N);
+        const int r = (int)(rb / nimg), b = (int)(rb - (long long)r * nimg);
+        Y[b * img_stride + (long long)rows[r] * N + o] = Zd[e];
+    }
+}
+
+template <typename real>
+__global__ void __launch_bounds__(256) dense_simt_kernel(int N, int nimg, const int* __restrict__ rows,
+                                                         const cplx<real>* __restrict__ W, const cplx<real>* __restrict__ Y,
+                                                         long long img_stride, cplx<real>* __restrict__ Zd) {
+    using C = cplx<real>;
+    __shared__ C Wt[32][33];
+    __shared__ C Yt[8][33];
+    const int r = blockIdx.x, o0 = blockIdx.y * 32;
+    const int oi = threadIdx.x & 31, bi = threadIdx.x >> 5;
+    const C* Wr = W + (size_t)r * N * N;
+    const long long row = rows[r];
+    for (int b0 = 0; b0 < nimg; b0 += 8) {
+        C acc = mk<real>(0, 0);
+        for (int i0 = 0; i0 < N; i0 += 32) {
+            for (int e = threadIdx.x; e < 32 * 32; e += 256) {
+                const int a = e >> 5, c = e & 31;
+                Wt[a][c] = (o0 + a < N && i0 + c < N) ? Wr[(size_t)(o0 + a) * N + i0 + c] : mk<real>(0, 0);
+            }
+            {
+                const int c = threadIdx.x & 31, bb = threadIdx.x >> 5;
+                Yt[bb][c] = (b0 + bb < nimg && i0 + c < N) ? Y[(b0 + bb) * img_stride + row * N + i0 + c] : mk<real>(0, 0);
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int c = 0; c < 32; ++c) acc = cfma(Wt[oi][c], Yt[bi][c], acc);
+            __syncthreads();
+        }
+        if (o0 + oi < N && b0 + bi < nimg) Zd[((size_t)r * nimg + b0 + bi) * N + o0 + oi] = acc;
+    }
+}
+
+// ------------------------------------------------------------------ tcgen05 (sm_100 family) helpers
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// shared-memory matrix descriptor: K-major, no swizzle; LBO = byte step between core matrices along K,
+// SBO = byte step between 8-row groups along M / N; bits 46-47 = 1 (descriptor version of tcgen05)
+__device__ __forceinline__ uint64_t desc_kmajor(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFF);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFF) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFF) << 32;
+    d |= (uint64_t)1 << 46;
+    return d;
+}
+
+__device__ __forceinline__ uint32_t to_tf32(float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return r;
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(tmem_d),
+        "l"(adesc), "l"(bdesc), "r"(idesc), "r"(acc));
+}
+
+// bounded wait on an mbarrier phase; returns false if the limit ran out
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+    for (long it = 0; it < (1L << 24); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+constexpr int TC_M = 128;   // real output rows per CTA (TMEM lanes)
+constexpr int TC_KC = 32;   // real K per chunk
+constexpr int TC_THREADS = 128;
+
+// A / X tile element (row, k) -> byte offset in the canonical K-major no-swizzle layout of a TC_KC-wide chunk:
+// core matrix (row/8, k/4) at ((row/8) * (TC_KC/4) + k/4) * 128, element ((row%8) * 16 + (k%4) * 4)
+// Threads fill one core matrix per warp instruction: lane -> (row%8 = lane/4, k%4 = lane%4), 128 contiguous bytes.
+
+template <int BP>
+__global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, const int* __restrict__ rows,
+                                                              const float2* __restrict__ W, const float2* __restrict__ Y,
+                                                              long long img_stride, float2* __restrict__ Zd,
+                                                              int* __restrict__ err) {
+    constexpr int A_BYTES = TC_M * TC_KC * 4;  // 16 KB
+    constexpr int X_BYTES = BP * TC_KC * 4;
+    constexpr int NCOLS = BP <= 32 ? 32 : (BP <= 64 ? 64 : (BP <= 128 ? 128 : 256));
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    unsigned char* a_hi = smem_raw;
+    unsigned char* a_lo = a_hi + A_BYTES;
+    unsigned char* x_hi = a_lo + A_BYTES;
+    unsigned char* x_lo = x_hi + X_BYTES;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(x_lo + X_BYTES);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+
+    const int r = blockIdx.x;
+    const int m0 = blockIdx.y * TC_M;   // first real output row of this CTA (0 .. 2N)
+    const int b0 = blockIdx.z * BP;     // first image of this CTA
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const float2* Wr = W + (size_t)r * N * N;
+    const long long yrow = (long long)rows[r] * N;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(NCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // instruction descriptor: D f32 (bits 4-5 = 1), A and B tf32 (bits 7-9, 10-12 = 2), both K-major,
+    // N >> 3 at bits 17-22, M >> 4 at bits 24-28
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BP >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
+    const int kchunks = (2 * N) / TC_KC;
+    bool ok = true;
+    // the tensor-core accumulator holds one K chunk; its partial sums are added into FP32 registers (CUDA cores,
+    // round to nearest) after every chunk, so accumulation error does not grow with K
+    float acc[BP];
+#pragma unroll
+    for (int q = 0; q < BP; ++q) acc[q] = 0.f;
+    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+    for (int kc = 0; kc < kchunks && ok; ++kc) {
+        const int kk0 = kc * TC_KC;
+        const int half = kk0 >= N ? 1 : 0;  // K half: 0 multiplies Re y, 1 multiplies Im y
+        const int i0 = kk0 - half * N;
+        // A tile: 128 rows x 32 k, one core matrix (8 rows x 4 k) per warp per iteration
+        for (int cm = warp; cm < (TC_M / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
+            const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
+            const int m = m0 + rg * 8 + (lane >> 2), kk = kg * 4 + (lane & 3);
+            const int outhalf = m >= N ? 1 : 0;
+            const float2 w = Wr[(size_t)(m - outhalf * N) * N + i0 + kk];
+            const float v = outhalf == 0 ? (half == 0 ? w.x : -w.y) : (half == 0 ? w.y : w.x);
+            const uint32_t hi = to_tf32(v);
+            const uint32_t lo = to_tf32(v - __uint_as_float(hi));
+            const int off = cm * 128 + lane * 4;
+            *reinterpret_cast<uint32_t*>(a_hi + off) = hi;
+            *reinterpret_cast<uint32_t*>(a_lo + off) = lo;
+        }
+        // X tile: BP rows (images) x 32 k
+        for (int cm = warp; cm < (BP / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
+            const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
+            const int b = b0 + rg * 8 + (lane >> 2), kk = kg * 4 + (lane & 3);
+            float v = 0.f;
+            if (b < nimg) {
+                const float2 y = Y[b * img_stride + yrow + i0 + kk];
+                v = half ? y.y : y.x;
+            }
+            const uint32_t hi = to_tf32(v);
+            const uint32_t lo = to_tf32(v - __uint_as_float(hi));
+            const int off = cm * 128 + lane * 4;
+            *reinterpret_cast<uint32_t*>(x_hi + off) = hi;
+            *reinterpret_cast<uint32_t*>(x_lo + off) = lo;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (threadIdx.x == 0) {
+#pragma unroll
+            for (int k8 = 0; k8 < TC_KC / 8; ++k8) {
+                const uint32_t koff = k8 * 256;  // two core matrices along K
+                const uint64_t ah = desc_kmajor(smem_addr(a_hi) + koff, 128, (TC_KC / 4) * 128);
+                const uint64_t al = desc_kmajor(smem_addr(a_lo) + koff, 128, (TC_KC / 4) * 128);
+                const uint64_t xh = desc_kmajor(smem_addr(x_hi) + koff, 128, (TC_KC / 4) * 128);
+                const uint64_t xl = desc_kmajor(smem_addr(x_lo) + koff, 128, (TC_KC / 4) * 128);
+                mma_tf32(tmem, ah, xh, idesc, k8 > 0 ? 1u : 0u);
+                mma_tf32(tmem, ah, xl, idesc, 1u);
+                mma_tf32(tmem, al, xh, idesc, 1u);
+            }
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
+                         : "memory");
+        }
+        // every thread waits until the tensor cores have consumed the tiles (and, after the last chunk, finished D)
+        const int waited = mbar_wait(smem_addr(mbar), (uint32_t)(kc & 1)) ? 1 : 0;
+        ok = __syncthreads_and(waited) != 0;  // uniform across the CTA
+        if (!ok) {
+            if (threadIdx.x == 0) atomicExch(err, 1);
+            break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int c0 = 0; c0 < BP; c0 += 16) {
+            uint32_t v[16];
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
+                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+                : "r"(trow + (uint32_t)c0));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 16; ++q) acc[c0 + q] += __uint_as_float(v[q]);
+        }
+        // the next chunk's MMAs overwrite the accumulator only after every warp has read it
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+    }
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+
+    if (ok) {
+        // output row m0 + 32 warp + lane, columns = images b0 ..
+        const int mrow = m0 + warp * 32 + lane;
+        const int outhalf = mrow >= N ? 1 : 0;
+        const int o = mrow - outhalf * N;
+        float* zf = reinterpret_cast<float*>(Zd);
+#pragma unroll
+        for (int q = 0; q < BP; ++q) {
+            const int b = b0 + q;
+            if (b < nimg) zf[(((size_t)r * nimg + b) * N + o) * 2 + outhalf] = acc[q];
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
+}
+
+template <int BP>
+static int launch_tc(int n, int nimg, int nrows, const int* rows, const void* W, const void* Y, long long img_stride,
+                     void* Zd, int* err, cudaStream_t st) {
+    const int N = 1 << n;
+    const size_t smem = 2 * (size_t)TC_M * TC_KC * 4 + 2 * (size_t)BP * TC_KC * 4 + 64;
+    auto kern = dense_tc_kernel<BP>;
+    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
+    dim3 grid(nrows, (2 * N) / TC_M, (nimg + BP - 1) / BP);
+    kern<<<grid, TC_THREADS, smem, st>>>(N, nimg, rows, reinterpret_cast<const float2*>(W),
+                                         reinterpret_cast<const float2*>(Y), img_stride, reinterpret_cast<float2*>(Zd), err);
+    return launch_status("dense_tc_kernel");
+}
+
+int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
+               void* Zd, int* err, int use_tc, cudaStream_t st) {
+    if ((dtype != ADRT_F32 && dtype != ADRT_F64) || n < 1 || n > 11 || nimg < 0 || nrows < 0 ||
+        (nimg && nrows && (!rows || !W || !Y || !Zd))) {
+        set_error("dense_rows: bad arguments (dtype=%d n=%d nimg=%d nrows=%d)", dtype, n, nimg, nrows);
+        return ADRT_EINVAL;
+    }
+    if (!nimg || !nrows) return ADRT_OK;
+    const int N = 1 << n;
+    int rc;
+    if (dtype == ADRT_F32 && use_tc && n >= 6) {
+        if (!err) { set_error("dense_rows: the tensor-core path needs an error flag"); return ADRT_EINVAL; }
+        if (nimg <= 16) rc = launch_tc<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        else if (nimg <= 32) rc = launch_tc<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        else rc = launch_tc<64>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+    } else {
+        dim3 grid(nrows, (N + 31) / 32);
+        if (dtype == ADRT_F32)
+            dense_simt_kernel<float><<<grid, 256, 0, st>>>(N, nimg, rows, reinterpret_cast<const float2*>(W),
+                                                           reinterpret_cast<const float2*>(Y), img_stride,
+                                                           reinterpret_cast<float2*>(Zd));
+        else
+            dense_simt_kernel<double><<<grid, 256, 0, st>>>(N, nimg, rows, reinterpret_cast<const double2*>(W),
+                                                            reinterpret_cast<const double2*>(Y), img_stride,
+                                                            reinterpret_cast<double2*>(Zd));
+        rc = launch_status("dense_simt_kernel");
+    }
+    if (rc) return rc;
+    const long long total = (long long)nrows * nimg * N;
+    int grid = (int)((total + 255) / 256);
+    if (grid > 65535 * 4) grid = 65535 * 4;
+    if (dtype == ADRT_F32)
+        dense_scatter_kernel<float2><<<grid, 256, 0, st>>>(N, nimg, nrows, rows, reinterpret_cast<const float2*>(Zd),
+                                                           reinterpret_cast<float2*>(Y), img_stride);
+    else
+        dense_scatter_kernel<double2><<<grid, 256, 0, st>>>(N, nimg, nrows, rows, reinterpret_cast<const double2*>(Zd),
+                                                            reinterpret_cast<double2*>(Y), img_stride);
+    return launch_status("dense_scatter_kernel");
+}
+
+}  // namespace adrt

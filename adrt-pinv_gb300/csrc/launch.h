@@ -29,5 +29,7 @@ int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, cons
                const double* xp, double* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
                const double* g1_coef, cudaStream_t st);
 int outer_step_max_n(int dtype);
+int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
+               void* Zd, int* err, int use_tc, cudaStream_t st);
 int cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, cudaStream_t st);
 }  // namespace adrt

@@ -55,6 +55,9 @@ class RowTables:
         self._dense_dev = {}
         self.count = 0  # level-rows applied, counted as the reference does
         self.timer = None  # list: when set, (start, end) CUDA events of every polynomial-row launch are appended
+        self.use_tc = real == torch.float32  # dense rows on tensor cores in FP32
+        self.err = torch.zeros(1, dtype=torch.int32, device=device)
+        self._zd = None
 
     def job(self, Y, ops, rows):
         p = self.plan
@@ -103,17 +106,27 @@ class RowTables:
                 tot += int(np.sum(np.maximum(d - 1, 0))) * 2 * (hi - lo + 1)
         return tot
 
-    def dense_table(self, fold_pre, fold_post):
-        key = (fold_pre, fold_post)
+    def dense_table(self, fold_pre, fold_post, pre_b1=False, post_b1t=False):
+        key = (fold_pre, fold_post, pre_b1, post_b1t)
         if key not in self._dense_dev:
-            T = self.plan.dense_operator(fold_pre, fold_post)
-            self._dense_dev[key] = torch.from_numpy(T[self.dense_sel]).to(device=self.device, dtype=_cdtype(self.real))
+            T = self.plan.dense_row_operator(fold_pre, fold_post, pre_b1, post_b1t)
+            self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T[self.dense_sel])).to(
+                device=self.device, dtype=_cdtype(self.real))
         return self._dense_dev[key]
+
+    def dense_apply(self, Y, T):
+        """Y[b, r] <- T_r Y[b, r] for the dense rows (tensor cores in FP32, CUDA cores in FP64)."""
+        B, R, N = Y.shape
+        nd = int(self.rows_dense.numel())
+        if self._zd is None or self._zd.shape[1] != B:
+            self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
+        C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(T), C.ptr(Y), R * N,
+               C.ptr(self._zd), C.ptr(self.err), 1 if self.use_tc else 0, C.stream_handle())
 
     def run(self, Y, ops):
         """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take the exact
-        filter (fastops.py:100-117), fused with the adjoint levels before it and the Gram levels after it into one
-        precomputed operator applied as a batched matrix product."""
+        filter (fastops.py:100-117), fused with the butterflies around it (adjoint levels before, Gram levels and
+        the level-1 butterflies of the hybrid around it) into one precomputed operator per row."""
         ops = fuse_ops(ops)
         B = Y.shape[0]
         if not ops:
@@ -139,14 +152,16 @@ class RowTables:
             fold_post = bool(post) and post[0] == ("M", plo, phi)
             if fold_post:
                 post = post[1:]
+            pre_b1 = pre == [("B", 1, 1)]
+            post_b1t = post == [("BT", 1, 1)]
+            if pre_b1:
+                pre = []
+            if post_b1t:
+                post = []
             self._timed_main(Y, ops, st)
             if pre:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, pre, self.rows_dense)), st)
-            T = self.dense_table(fold_pre, fold_post)
-            rd = self.rows_dense.long()
-            Yd = Y.index_select(1, rd)  # (B, 2Kd, N)
-            Zd = torch.bmm(T, Yd.permute(1, 2, 0))  # (2Kd, N, B)
-            Y.index_copy_(1, rd, Zd.permute(2, 0, 1))
+            self.dense_apply(Y, self.dense_table(fold_pre, fold_post, pre_b1, post_b1t))
             if post:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, post, self.rows_dense)), st)
         self.count += B * self.plan.level_rows(ops_unfused(ops))

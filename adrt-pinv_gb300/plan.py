@@ -169,6 +169,23 @@ class Plan:
         self.dense_tables = out
         return out
 
+    def dense_row_operator(self, fold_pre_adjoint, fold_post_gram, pre_b1, post_b1t):
+        """dense_operator with the level-1 butterfly of the hybrid folded in as well: right-multiplied by B_1 when the
+        op list applies B(1,1) before the filter, left-multiplied by B_1^* when it applies BT(1,1) after it
+        (fastops.py:330, 335), so that each dense row of an op list is one matrix. (Kd, N, N) complex, FP64."""
+        T = self.dense_operator(fold_pre_adjoint, fold_post_gram)
+        if T is None or not (pre_b1 or post_b1t):
+            return T
+        z = roots_of_unity(self.L)[self.dense_freqs]
+        out = T.copy()
+        for i, zk in enumerate(z):
+            B1 = _butterfly_matrix(self.n, zk, 1, 1)
+            if pre_b1:
+                out[i] = out[i] @ B1
+            if post_b1t:
+                out[i] = B1.conj().T @ out[i]
+        return out
+
     def dense_operator(self, fold_pre_adjoint, fold_post_gram):
         """Per dense frequency, the exact operator that replaces the filter op of an op list together with the
         butterflies around it: F_k, F_k A_k^* (filter after the adjoint levels, as in the back-projections) or

@@ -161,6 +161,14 @@ int adrt_outer_step(int dtype, int n, int nimg, const double* y, const void* p0,
                     int precond, int g1_deg, const double* g1_coef, void* stream);
 int adrt_outer_step_max_n(int dtype);
 
+/* Dense low-frequency rows (fastops.py:28-40, 100-117): for r < nrows and every image b,
+ *   Y[b, rows[r], :] <- W_r Y[b, rows[r], :]     (W: nrows x N x N complex, row-major, dtype; Y rows of N complex at
+ *   image stride img_stride complex elements), computed out of place in Zd (nrows x nimg x N complex scratch) and
+ * copied back. use_tc = 1 with FP32 and n >= 6: tensor cores (tcgen05.mma kind::tf32, 3xTF32 split, FP32 accumulate);
+ * *err (device int) is set to 1 if a tensor-core completion wait ran out. Otherwise CUDA cores. */
+int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
+                    long long img_stride, void* Zd, int32_t* err, int use_tc, void* stream);
+
 /* Spatial ADRT in the reference's sinogram layout (adrtcore.py:122-137), nimg images, exact for integer dtypes
  * (ADRT_I32, ADRT_I64; sums only), FP32 / FP64 otherwise. scratch: 2 * nimg * 4 * (2N-1) * N elements of dtype.
  * forward: x (nimg x N x N) -> b (nimg x 4 x (2N-1) x N); transpose: b -> x. */

@@ -1,0 +1,46 @@
+"""Dense low-frequency rows (adrt_dense_rows): tensor-core 3xTF32 kernel and CUDA-core kernel against an FP64
+NumPy product, through the C ABI. 3xTF32 with per-chunk promotion to FP32 registers keeps FP32 accuracy: the
+norm-wise relative error of every output row is at most 5e-7 (1e-6 for the CUDA-core kernel's sequential sums)."""
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,nimg,nrows", [(8, 64, 6), (6, 5, 3), (9, 20, 2), (7, 100, 2)])
+def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
+    import torch
+
+    C = pkg._lib
+    C.load()
+    N, R = 1 << n, 16
+    rng = np.random.default_rng(n)
+    W = (rng.standard_normal((nrows, N, N)) + 1j * rng.standard_normal((nrows, N, N))) / np.sqrt(N)
+    Y = rng.standard_normal((nimg, R, N)) + 1j * rng.standard_normal((nimg, R, N))
+    rows = np.array(sorted(rng.choice(R, nrows, replace=False)), dtype=np.int32)
+    ref = Y.copy()
+    for i, r in enumerate(rows):
+        ref[:, r, :] = Y[:, r, :] @ W[i].T
+    for use_tc in (1, 0):
+        Wd = torch.from_numpy(W).to("cuda", torch.complex64)
+        Yd = torch.from_numpy(Y).to("cuda", torch.complex64)
+        rd = torch.from_numpy(rows).cuda()
+        Zd = torch.empty((nrows, nimg, N), dtype=torch.complex64, device="cuda")
+        err = torch.zeros(1, dtype=torch.int32, device="cuda")
+        C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(Wd), C.ptr(Yd), R * N, C.ptr(Zd), C.ptr(err),
+               use_tc, C.stream_handle())
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        out = Yd.cpu().numpy()
+        for r in range(R):
+            e = np.linalg.norm(out[:, r, :] - ref[:, r, :]) / np.linalg.norm(ref[:, r, :])
+            assert e < (5e-7 if use_tc else 1e-6), (use_tc, r, e)  # sequential FP32 sum over K = 2N on CUDA cores
+    # FP64 CUDA-core path
+    Wd = torch.from_numpy(W).cuda()
+    Yd = torch.from_numpy(Y).cuda()
+    Zd = torch.empty((nrows, nimg, N), dtype=torch.complex128, device="cuda")
+    C.call("adrt_dense_rows", C.F64, n, nimg, nrows, C.ptr(torch.from_numpy(rows).cuda()), C.ptr(Wd), C.ptr(Yd), R * N,
+           C.ptr(Zd), None, 0, C.stream_handle())
+    torch.cuda.synchronize()
+    assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
