@@ -7,12 +7,13 @@
 //     [Re z; Im z] (2N x B) = [[Re W, -Im W], [Im W, Re W]] (2N x 2N) . [Re y; Im y] (2N x B),
 // on tcgen05.mma kind::tf32 with the 3xTF32 split (a = a_hi + a_lo, products hi.hi + hi.lo + lo.hi, FP32 accumulation
 // in tensor memory): about FP32 accuracy, which these rows need (they carry most of the image energy). One CTA per
-// (dense row, 128 real output rows, batch tile); K in chunks of 32: the threads convert and store A / X tiles into
-// shared memory in the canonical K-major layout without swizzle (8-row x 16-byte core matrices, 128 B apart along K,
-// 1024 B apart along M / N), one thread issues 12 MMAs per chunk and commits them to an mbarrier that every thread
-// waits on (bounded) before the tiles are overwritten. The tensor-memory accumulator holds one chunk only: after every
-// chunk the four warps read its 128 lanes (tcgen05.ld) and add them into FP32 registers, because accumulating all of K
-// in tensor memory measured 2e-6..7e-6 relative error growing with K (truncating accumulation), against 1e-7 here.
+// (dense row, 128 real output rows, batch tile of <= 64 images); K in chunks of 32 through two stages: the threads
+// convert and store the A / X tiles of chunk k+1 into shared memory (canonical K-major layout without swizzle:
+// 8-row x 16-byte core matrices, 128 B apart along K, 1024 B apart along M / N) while the tensor cores run chunk k;
+// one thread issues 12 MMAs per chunk into one of two tensor-memory accumulators and commits them to that stage's
+// mbarrier, on which every thread waits (bounded) before reusing the stage. Each accumulator holds one chunk only:
+// the warps read it back (tcgen05.ld) and add it into FP32 registers, because accumulating all of K in tensor memory
+// measured 2e-6..7e-6 relative error growing with K (truncating accumulation), against 1e-7 this way.
 //
 // CUDA-core kernel: the same product for any N and for FP64.
 #include "common.cuh"
@@ -105,13 +106,13 @@ __device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
 }
 
 constexpr int TC_M = 128;   // real output rows per CTA (TMEM lanes)
-constexpr int TC_KC = 32;   // real K per chunk
-constexpr int TC_THREADS = 128;
+constexpr int TC_KC = 32;   // real K per chunk (16 complex columns of W)
+constexpr int TC_THREADS = 256;
 
-// A / X tile element (row, k) -> byte offset in the canonical K-major no-swizzle layout of a TC_KC-wide chunk:
-// core matrix (row/8, k/4) at ((row/8) * (TC_KC/4) + k/4) * 128, element ((row%8) * 16 + (k%4) * 4)
-// Threads fill one core matrix per warp instruction: lane -> (row%8 = lane/4, k%4 = lane%4), 128 contiguous bytes.
-
+// Tiles in the canonical K-major no-swizzle layout of a TC_KC-wide chunk: element (row, k) at byte
+// ((row/8) * (TC_KC/4) + k/4) * 128 + (row%8) * 16 + (k%4) * 4. K is interleaved by complex column:
+// k = 2 (i - i0) + c multiplies Re y_i (c = 0) or Im y_i (c = 1), so A row m reads whole complex entries of W.
+// Warps fill one core matrix per instruction: lane -> (row%8 = lane/4, k%4 = lane%4), 128 contiguous bytes.
 template <int BP>
 __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, const int* __restrict__ rows,
                                                               const float2* __restrict__ W, const float2* __restrict__ Y,
@@ -119,18 +120,16 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
                                                               int* __restrict__ err) {
     constexpr int A_BYTES = TC_M * TC_KC * 4;  // 16 KB
     constexpr int X_BYTES = BP * TC_KC * 4;
-    constexpr int NCOLS = BP <= 32 ? 32 : (BP <= 64 ? 64 : (BP <= 128 ? 128 : 256));
+    constexpr int STAGE = 2 * A_BYTES + 2 * X_BYTES;
+    constexpr int NCOLS = 2 * BP <= 32 ? 32 : (2 * BP <= 64 ? 64 : 128);  // two accumulators of BP columns
+    constexpr int HB = BP / 2;                                             // columns promoted per warp
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    unsigned char* a_hi = smem_raw;
-    unsigned char* a_lo = a_hi + A_BYTES;
-    unsigned char* x_hi = a_lo + A_BYTES;
-    unsigned char* x_lo = x_hi + X_BYTES;
-    uint64_t* mbar = reinterpret_cast<uint64_t*>(x_lo + X_BYTES);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 1);
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + 2 * STAGE);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
 
     const int r = blockIdx.x;
-    const int m0 = blockIdx.y * TC_M;   // first real output row of this CTA (0 .. 2N)
-    const int b0 = blockIdx.z * BP;     // first image of this CTA
+    const int m0 = blockIdx.y * TC_M;  // first real output row of this CTA (0 .. 2N)
+    const int b0 = blockIdx.z * BP;    // first image of this CTA
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const float2* Wr = W + (size_t)r * N * N;
     const long long yrow = (long long)rows[r] * N;
@@ -141,7 +140,8 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(mbar)));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -153,38 +153,63 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
     // N >> 3 at bits 17-22, M >> 4 at bits 24-28
     const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BP >> 3) << 17) | ((uint32_t)(TC_M >> 4) << 24);
     const int kchunks = (2 * N) / TC_KC;
-    bool ok = true;
-    // the tensor-core accumulator holds one K chunk; its partial sums are added into FP32 registers (CUDA cores,
-    // round to nearest) after every chunk, so accumulation error does not grow with K
-    float acc[BP];
+    // warps w and w + 4 read the same 32 accumulator lanes (rows), each half of the columns
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const int col0 = (warp >> 2) * HB;
+    float acc[HB];
 #pragma unroll
-    for (int q = 0; q < BP; ++q) acc[q] = 0.f;
-    const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
-    for (int kc = 0; kc < kchunks && ok; ++kc) {
-        const int kk0 = kc * TC_KC;
-        const int half = kk0 >= N ? 1 : 0;  // K half: 0 multiplies Re y, 1 multiplies Im y
-        const int i0 = kk0 - half * N;
-        // A tile: 128 rows x 32 k, one core matrix (8 rows x 4 k) per warp per iteration
+    for (int q = 0; q < HB; ++q) acc[q] = 0.f;
+    bool ok = true;
+
+    // add one chunk's partial sums (accumulator s) into the FP32 registers
+    auto promote = [&](int s) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+        for (int c = 0; c < HB; c += 8) {
+            uint32_t v[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7])
+                         : "r"(tmem + lane_base + (uint32_t)(s * BP + col0 + c)));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 8; ++q) acc[c + q] += __uint_as_float(v[q]);
+        }
+    };
+
+    for (int kc = 0; kc < kchunks; ++kc) {
+        const int s = kc & 1;
+        unsigned char* a_hi = smem_raw + s * STAGE;
+        unsigned char* a_lo = a_hi + A_BYTES;
+        unsigned char* x_hi = a_lo + A_BYTES;
+        unsigned char* x_lo = x_hi + X_BYTES;
+        if (kc >= 2) {
+            // chunk kc-2 used this stage and accumulator: wait for its MMAs, fold its partial in
+            const int waited = mbar_wait(smem_addr(&mbar[s]), (uint32_t)(((kc - 2) >> 1) & 1)) ? 1 : 0;
+            ok = __syncthreads_and(waited) != 0;
+            if (!ok) break;
+            promote(s);
+        }
+        const int i0 = kc * (TC_KC / 2);
         for (int cm = warp; cm < (TC_M / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
             const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
-            const int m = m0 + rg * 8 + (lane >> 2), kk = kg * 4 + (lane & 3);
+            const int m = m0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
             const int outhalf = m >= N ? 1 : 0;
-            const float2 w = Wr[(size_t)(m - outhalf * N) * N + i0 + kk];
-            const float v = outhalf == 0 ? (half == 0 ? w.x : -w.y) : (half == 0 ? w.y : w.x);
+            const float2 w = Wr[(size_t)(m - outhalf * N) * N + i0 + (k >> 1)];
+            const int c = k & 1;
+            const float v = outhalf == 0 ? (c == 0 ? w.x : -w.y) : (c == 0 ? w.y : w.x);
             const uint32_t hi = to_tf32(v);
             const uint32_t lo = to_tf32(v - __uint_as_float(hi));
             const int off = cm * 128 + lane * 4;
             *reinterpret_cast<uint32_t*>(a_hi + off) = hi;
             *reinterpret_cast<uint32_t*>(a_lo + off) = lo;
         }
-        // X tile: BP rows (images) x 32 k
         for (int cm = warp; cm < (BP / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
             const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
-            const int b = b0 + rg * 8 + (lane >> 2), kk = kg * 4 + (lane & 3);
+            const int b = b0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
             float v = 0.f;
             if (b < nimg) {
-                const float2 y = Y[b * img_stride + yrow + i0 + kk];
-                v = half ? y.y : y.x;
+                const float2 y = Y[b * img_stride + yrow + i0 + (k >> 1)];
+                v = (k & 1) ? y.y : y.x;
             }
             const uint32_t hi = to_tf32(v);
             const uint32_t lo = to_tf32(v - __uint_as_float(hi));
@@ -193,9 +218,11 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
             *reinterpret_cast<uint32_t*>(x_lo + off) = lo;
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         __syncthreads();
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         if (threadIdx.x == 0) {
+            const uint32_t d = tmem + (uint32_t)(s * BP);
 #pragma unroll
             for (int k8 = 0; k8 < TC_KC / 8; ++k8) {
                 const uint32_t koff = k8 * 256;  // two core matrices along K
@@ -203,48 +230,34 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
                 const uint64_t al = desc_kmajor(smem_addr(a_lo) + koff, 128, (TC_KC / 4) * 128);
                 const uint64_t xh = desc_kmajor(smem_addr(x_hi) + koff, 128, (TC_KC / 4) * 128);
                 const uint64_t xl = desc_kmajor(smem_addr(x_lo) + koff, 128, (TC_KC / 4) * 128);
-                mma_tf32(tmem, ah, xh, idesc, k8 > 0 ? 1u : 0u);
-                mma_tf32(tmem, ah, xl, idesc, 1u);
-                mma_tf32(tmem, al, xh, idesc, 1u);
+                mma_tf32(d, ah, xh, idesc, k8 > 0 ? 1u : 0u);
+                mma_tf32(d, ah, xl, idesc, 1u);
+                mma_tf32(d, al, xh, idesc, 1u);
             }
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_addr(mbar))
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&mbar[s]))
                          : "memory");
         }
-        // every thread waits until the tensor cores have consumed the tiles (and, after the last chunk, finished D)
-        const int waited = mbar_wait(smem_addr(mbar), (uint32_t)(kc & 1)) ? 1 : 0;
-        ok = __syncthreads_and(waited) != 0;  // uniform across the CTA
-        if (!ok) {
-            if (threadIdx.x == 0) atomicExch(err, 1);
-            break;
-        }
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-#pragma unroll
-        for (int c0 = 0; c0 < BP; c0 += 16) {
-            uint32_t v[16];
-            asm volatile(
-                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-                : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]),
-                  "=r"(v[8]), "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
-                : "r"(trow + (uint32_t)c0));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int q = 0; q < 16; ++q) acc[c0 + q] += __uint_as_float(v[q]);
-        }
-        // the next chunk's MMAs overwrite the accumulator only after every warp has read it
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
     }
-    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-
+    // drain: the last two chunks
     if (ok) {
-        // output row m0 + 32 warp + lane, columns = images b0 ..
-        const int mrow = m0 + warp * 32 + lane;
+        for (int kc = kchunks - 2 > 0 ? kchunks - 2 : 0; kc < kchunks; ++kc) {
+            const int s = kc & 1;
+            const int waited = mbar_wait(smem_addr(&mbar[s]), (uint32_t)((kc >> 1) & 1)) ? 1 : 0;
+            ok = __syncthreads_and(waited) != 0;
+            if (!ok) break;
+            promote(s);
+        }
+    }
+    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    if (ok) {
+        const int mrow = m0 + (warp & 3) * 32 + lane;
         const int outhalf = mrow >= N ? 1 : 0;
         const int o = mrow - outhalf * N;
         float* zf = reinterpret_cast<float*>(Zd);
 #pragma unroll
-        for (int q = 0; q < BP; ++q) {
-            const int b = b0 + q;
+        for (int q = 0; q < HB; ++q) {
+            const int b = b0 + col0 + q;
             if (b < nimg) zf[(((size_t)r * nimg + b) * N + o) * 2 + outhalf] = acc[q];
         }
     }
@@ -257,7 +270,7 @@ template <int BP>
 static int launch_tc(int n, int nimg, int nrows, const int* rows, const void* W, const void* Y, long long img_stride,
                      void* Zd, int* err, cudaStream_t st) {
     const int N = 1 << n;
-    const size_t smem = 2 * (size_t)TC_M * TC_KC * 4 + 2 * (size_t)BP * TC_KC * 4 + 64;
+    const size_t smem = 2 * (2 * (size_t)TC_M * TC_KC * 4 + 2 * (size_t)BP * TC_KC * 4) + 64;
     auto kern = dense_tc_kernel<BP>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(nrows, (2 * N) / TC_M, (nimg + BP - 1) / BP);
