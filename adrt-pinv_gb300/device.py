@@ -292,6 +292,58 @@ class Pipeline:
         self.packed_sino(b, self.ops["BP"])
         return self.sum_parts(y)
 
+    # ---------------------------------------------------------------- CUDA graph of a whole apply
+    def device_bytes(self):
+        """Device memory held by this pipeline (buffers and tables)."""
+        t = self.tables
+        bufs = [self.Y, self.parts, self.y, self.s, *self.xs, *self.st, t.roots, t.deg, t.coef, t.rows_main,
+                t.rows_dense, *t._dense_dev.values()]
+        if t._zd is not None:
+            bufs.append(t._zd)
+        if getattr(self, "b_in", None) is not None:
+            bufs.append(self.b_in)
+        return sum(x.numel() * x.element_size() for x in bufs)
+
+    @staticmethod
+    def estimate_bytes(plan: Plan, batch, precision="fp32", stencil_precision=None, captured=True):
+        """Device bytes a pipeline for (plan, batch, precision) holds once it has run apply (and capture, which adds
+        the input buffer): the buffers of __init__, the two folded dense-row tables (filter of G and of the
+        backprojection) and the dense-row staging, computed without allocating anything."""
+        N, L, B = plan.N, plan.L, int(batch)
+        rs = PRECISIONS[precision].itemsize
+        ss = PRECISIONS[stencil_precision or precision].itemsize
+        nd = 2 * len(plan.dense_freqs)
+        img = B * N * N
+        total = B * 2 * L * N * 2 * rs + 3 * img * rs + 4 * img * 8 + 4 * img * ss
+        total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
+        total += L * 2 * rs + 3 * L * 4 + plan.coef.size * rs  # roots; deg and the row lists; coefficients
+        if captured:
+            total += B * 4 * (2 * N - 1) * N * 8
+        return int(total)
+
+    def capture(self):
+        """Record apply() on a private input buffer into a CUDA graph (after one eager warm-up run, so that every
+        lazily built table and kernel attribute exists). replay(b) then copies b in and replays the graph."""
+        N = self.plan.N
+        self.b_in = torch.zeros((self.B, 4, 2 * N - 1, N), dtype=torch.float64, device=self.device)
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            self.apply(self.b_in)
+            side.synchronize()
+            self.graph = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph, stream=side):
+                self.x_out = self.apply(self.b_in)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        return self
+
+    def replay(self, b=None):
+        """Run the captured apply on the current stream (b copied into the graph's input buffer first)."""
+        if b is not None:
+            self.b_in.copy_(b, non_blocking=True)
+        self.graph.replay()
+        return self.x_out
+
     def apply(self, b):
         """x = L b for B sinograms b (B, 4, 2N-1, N) on device; returns the FP64 (B, N, N) result buffer (a view
         of internal storage, valid until the next call)."""

@@ -194,6 +194,32 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def single_image_rates(H, b_dev, steps, torch):
+    """Reconstructions/s of one sinogram at a time on the device: eager Pipeline.apply at batch 1 (the plain
+    single-image GPU path) and the same apply replayed from a CUDA graph."""
+    pipe = H.pipeline(1)
+    b1 = b_dev[:1].contiguous()
+    for _ in range(3):
+        pipe.apply(b1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        pipe.apply(b_dev[i % b_dev.shape[0]:][:1])
+    torch.cuda.synchronize()
+    eager = steps / (time.perf_counter() - t0)
+    pipe.capture()
+    for _ in range(3):
+        pipe.replay(b1)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(steps):
+        pipe.replay(b_dev[i % b_dev.shape[0]:][:1])
+    torch.cuda.synchronize()
+    graph = steps / (time.perf_counter() - t0)
+    return {"eager_recon_s": eager, "graph_recon_s": graph, "unit": "recon/s",
+            "how": f"{steps} single sinograms, device-resident, host clock around the loop"}
+
+
 def run_ours(args):
     import torch
     import torch.distributed as dist
@@ -275,6 +301,10 @@ def run_ours(args):
         dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
     e2e_value = B * world / float(e2e_t.item())
 
+    # ---- the plain single-image GPU path (batch 1, eager launches) and the same under a CUDA graph
+    single = single_image_rates(H, b_dev, args.steps, torch)
+    barrier()
+
     if rank != 0:
         if world > 1:
             dist.destroy_process_group()
@@ -287,6 +317,7 @@ def run_ours(args):
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded ellipse phantoms + Gaussian noise)",
             "config": config(args, world), "gpu_launches": int(launches),
             "clocks": clk.summary(),
+            "single_image": single, "batched_over_single_image": value / world / single["eager_recon_s"],
             "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": int(b_host.numel() * 8),
                     "d2h_bytes_per_step": int(out_host.numel() * 8)}}
     if rows_launch_ms:
