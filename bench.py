@@ -9,7 +9,7 @@ needed between steps.
   value : device-resident sinograms, K timed steps of Pipeline.apply (CUDA events, barrier + sync both sides).
   e2e   : the public API FastHybridGpu.apply on pinned host sinograms with the result read back to pinned host
           memory every step (H2D + D2H inside the timed region).
-  roofline : the row engine (rows_fast_kernel), the dominant kernel, timed live with CUDA events on its stream;
+  roofline : the row engine (rows_prog_kernel), the dominant kernel, timed live with CUDA events on its stream;
           algorithmic FLOPs = level-rows x 8N (the reference's cost unit, fastops.py:166); peak = FP32 FMA
           throughput measured in this run by the library's probe kernel.
   cpu_baseline : the reference's C++-engine path (FastHybridCpp semantics: C row kernels + NumPy) timed on this
@@ -143,7 +143,7 @@ def cpu_reference_time(n, plan_kw, b_one, reps, threads):
 
 def traffic_per_launch():
     """DRAM bytes per launch of the row kernel from the committed ncu summary (null when not captured)."""
-    path = os.path.join(REPO, "profiles", "rows_fast_kernel_hybrid_n8_b64.txt")
+    path = os.path.join(REPO, "profiles", "rows_prog_kernel_hybrid_n8_b64_dram.txt")
     try:
         for line in open(path):
             if line.startswith("dram_bytes_per_launch:"):
@@ -322,8 +322,9 @@ def run_ours(args):
                     "d2h_bytes_per_step": int(out_host.numel() * 8)}}
     if rows_launch_ms:
         achieved = flops_per_launch / (rows_launch_ms * 1e-3) / 1e12
-        tr = traffic_per_launch()
-        line["roofline"] = {"bound": "fp32", "kernel": "rows_fast_kernel (G_h op list, polynomial rows)",
+        tr = traffic_per_launch()  # captured at N=256, batch 64; rows scale with the batch
+        tr = tr * B / 64 if tr is not None and n == 8 else None
+        line["roofline"] = {"bound": "fp32", "kernel": "rows_prog_kernel (G_h op list, polynomial rows)",
                             "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved * 1e12 / peak,
                             "peak_source": "measured in this run: FP32 FMA probe kernel",
                             "flop_per_launch": flops_per_launch, "launch_ms": rows_launch_ms,
