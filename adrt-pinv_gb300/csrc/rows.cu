@@ -1,8 +1,9 @@
 // Row engine: per offset-frequency row, the butterflies B_m (levels lo..hi), their adjoints and the fused Chebyshev
 // filter z = p_k(M) y, M = B^* B (reference: cpp/oblique.cpp:22-104, fastops.RowEngine fastops.py:70-138).
 //
-// Fast kernel (n <= 8). A row of N = 2^n complex values is held in registers by a group of T = 2^(n-r) lanes, each
-// holding R = 2^r values, r = ceil(n/2). Butterflies run in place: level m pairs the values whose physical index
+// Fast kernel (n <= 8; the compile-time programs also n = 9 in FP32). A row of N = 2^n complex values is held in
+// registers by a group of T = 2^(n-r) lanes, each holding R = 2^r values, r = ceil(n/2) (r = 4 at n = 9, where the
+// one index bit neither layout holds in registers, bit 4, is a warp-shuffle level). Butterflies run in place: level m pairs the values whose physical index
 // differs in bit m-1, with twiddles z^t, z^(t+1), t = bitrev_{m-1}(p mod 2^(m-1)); in-place forward levels leave the
 // row in bit-reversed order and the adjoint levels restore it, so an M = B^* B application needs no permutation.
 // Two register layouts cover the index bits:
@@ -15,6 +16,7 @@
 // Simple kernel (any n <= 11, any lo): one CTA per row, the row in shared memory in natural order, ping-pong
 // levels exactly as cpp/oblique.cpp:22-51. Used for op lists the fast kernel does not cover.
 #include <cstdio>
+#include <type_traits>
 
 #include "common.cuh"
 #include "launch.h"
@@ -34,17 +36,22 @@ template <typename real> struct TwSrc {
 
 template <int n> struct FastCfg {
     static constexpr int N = 1 << n;
-    static constexpr int r = (n + 1) / 2;
+    // register bits r = ceil(n/2) up to n = 8; n = 9 keeps 16 values per lane (a whole warp per row), so index bit 4
+    // is held by neither layout's registers and runs as a warp-shuffle level in the A layout (lane u ^ 1)
+    static constexpr int r = n == 9 ? 4 : (n + 1) / 2;
     static constexpr int R = 1 << r;
     static constexpr int tb = n - r;
     static constexpr int T = 1 << tb;
-    static constexpr int NB = (n > r) ? ((1 << (r - tb)) * ((1 << (n - r)) - 1)) : 0;
+    static constexpr int BLO = imax(r, tb);  // the B layout's registers hold index bits BLO..n-1
+    static constexpr int MID = BLO - r;      // shuffle levels r+1..BLO
+    static_assert(T <= 32 && MID <= 1, "row group must fit one warp, with at most one shuffle level");
+    static constexpr int NB = (n > BLO) ? ((1 << (BLO - tb)) * ((1 << (n - BLO)) - 1)) : 0;
     static constexpr int SW_SHIFT = imax(r, 4);
     static constexpr int SW_MASK = (1 << imin(r - 1, 3)) - 1;
     static constexpr int PAD = (T < 16) ? 8 : 0;
     static constexpr int BUF = N + PAD;
     __host__ __device__ static constexpr int phys(int p) { return p ^ (((p >> SW_SHIFT) & SW_MASK) << 1); }
-    __host__ __device__ static constexpr int offB(int b) { return (1 << (r - tb)) * ((1 << (b - r)) - 1); }
+    __host__ __device__ static constexpr int offB(int b) { return (1 << (BLO - tb)) * ((1 << (b - BLO)) - 1); }
 };
 
 // pair store/load at an even physical index (16 B for float, 2 x 16 B for double)
@@ -102,7 +109,7 @@ template <typename C, int n> struct Lanes {
     __device__ __forceinline__ static void fwdB(C (&v)[R], const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], int lo,
                                                 int hi) {
 #pragma unroll
-        for (int b = r; b < n; ++b) {
+        for (int b = F::BLO; b < n; ++b) {
             if (b + 1 >= lo && b + 1 <= hi) {
                 const int jb = b - tb;
 #pragma unroll
@@ -119,7 +126,7 @@ template <typename C, int n> struct Lanes {
     __device__ __forceinline__ static void adjB(C (&v)[R], const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], int lo,
                                                 int hi) {
 #pragma unroll
-        for (int b = n - 1; b >= r; --b) {
+        for (int b = n - 1; b >= F::BLO; --b) {
             if (b + 1 >= lo && b + 1 <= hi) {
                 const int jb = b - tb;
 #pragma unroll
@@ -130,6 +137,40 @@ template <typename C, int n> struct Lanes {
                     v[j] = cadd(g0, g1);
                     v[j | (1 << jb)] = cdot2c(t0[idx], g0, t1[idx], g1);
                 }
+            }
+        }
+    }
+    // z^t for t <= R: tA holds t <= R/2, the rest is z^(R/2) z^(t - R/2) (t is a compile-time constant here)
+    __device__ __forceinline__ static C twx(const C (&tA)[R / 2 + 1], int t) {
+        return t <= R / 2 ? tA[t] : cmul(tA[R / 2], tA[t - R / 2]);
+    }
+    // the shuffle level (index bit r, level r+1) in the A layout, p = j + R u: the pair partner of slot j is slot j
+    // of lane u ^ 1, and the twiddle index t = bitrev_r(j) is the same in every lane
+    __device__ __forceinline__ static void fwdM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u) {
+        if (F::MID && r + 1 >= lo && r + 1 <= hi) {
+            const bool upper = u & 1;
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const int t = brev(j, r);
+                C o;
+                o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1);
+                o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1);
+                const C f0 = upper ? o : v[j], f1 = upper ? v[j] : o;
+                v[j] = cfma(upper ? twx(tA, t + 1) : twx(tA, t), f1, f0);
+            }
+        }
+    }
+    __device__ __forceinline__ static void adjM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u) {
+        if (F::MID && r + 1 >= lo && r + 1 <= hi) {
+            const bool upper = u & 1;
+#pragma unroll
+            for (int j = 0; j < R; ++j) {
+                const int t = brev(j, r);
+                C o;
+                o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1);
+                o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1);
+                const C g0 = upper ? o : v[j], g1 = upper ? v[j] : o;
+                v[j] = upper ? cdot2c(twx(tA, t), g0, twx(tA, t + 1), g1) : cadd(g0, g1);
             }
         }
     }
@@ -156,6 +197,7 @@ template <typename C, int n> struct Lanes {
                                                const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm) {
         fwdA(v, tA, lo, hi);
         if (hi > r) {
+            fwdM(v, tA, lo, hi, u);
             toB(v, buf, u, gm);
             fwdB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
@@ -167,6 +209,7 @@ template <typename C, int n> struct Lanes {
             toB(v, buf, u, gm);
             adjB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
+            adjM(v, tA, lo, hi, u);
         }
         adjA(v, tA, lo, hi);
     }
@@ -174,10 +217,12 @@ template <typename C, int n> struct Lanes {
                                                 const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm) {
         fwdA(v, tA, lo, hi);
         if (hi > r) {
+            fwdM(v, tA, lo, hi, u);
             toB(v, buf, u, gm);
             fwdB(v, t0, t1, lo, hi);
             adjB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
+            adjM(v, tA, lo, hi, u);
         }
         adjA(v, tA, lo, hi);
     }
@@ -228,7 +273,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (NB) {
                 const int U = tb ? (int)(__brev((unsigned)u) >> (32 - tb)) : 0;
 #pragma unroll
-                for (int b = r; b < n; ++b) {
+                for (int b = F::BLO; b < n; ++b) {
                     const int jb = b - tb;
 #pragma unroll
                     for (int vv = 0; vv < (1 << jb); ++vv) {
@@ -369,6 +414,7 @@ template <typename C, int n> struct CtLanes {
             }
         }
         if (HI > r) {
+            Ln::fwdM(dst, tA, LO, HI, u);
             Ln::toB(dst, buf, u, gm);
             Ln::fwdB(dst, t0, t1, LO, HI);
         }
@@ -382,6 +428,7 @@ template <typename C, int n> struct CtLanes {
         if (HI > r) {
             Ln::adjB(dst, t0, t1, LO, HI);
             Ln::toA(dst, buf, u, gm);
+            Ln::adjM(dst, tA, LO, HI, u);
         }
         Ln::adjA(dst, tA, LO, HI);
     }
@@ -435,7 +482,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             if (NB) {
                 const int U = tb ? (int)(__brev((unsigned)u) >> (32 - tb)) : 0;
 #pragma unroll
-                for (int b = r; b < n; ++b) {
+                for (int b = F::BLO; b < n; ++b) {
                     const int jb = b - tb;
 #pragma unroll
                     for (int vv = 0; vv < (1 << jb); ++vv) {
@@ -709,8 +756,7 @@ static int launch_simple(const adrt_row_job& J, const TwSrc<real>& tw, int total
 
 // the register kernel runs in-place levels with lo <= 2 and needs every op but a leading adjoint / trailing forward
 // to start and end in natural order (B with hi >= 2 only last, BT with hi >= 2 only first)
-static bool fast_ok(const adrt_row_job& J) {
-    if (J.n < 1 || J.n > 8) return false;
+static bool fast_levels_ok(const adrt_row_job& J) {
     for (int o = 0; o < J.nops; ++o) {
         if (J.lo[o] > 2) return false;
         if (J.op[o] == ADRT_OP_B && J.hi[o] >= 2 && o != J.nops - 1) return false;
@@ -718,6 +764,8 @@ static bool fast_ok(const adrt_row_job& J) {
     }
     return true;
 }
+
+static bool fast_ok(const adrt_row_job& J) { return J.n >= 1 && J.n <= 8 && fast_levels_ok(J); }
 
 template <typename real, int n>
 static int launch_prog(const adrt_row_job& J, const TwSrc<real>& tw, int total, int prog, cudaStream_t st) {
@@ -764,7 +812,9 @@ static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double
         return ADRT_EINVAL;
     }
     const int total = (int)total_l;
-    const int prog = (!pout && fast_ok(J)) ? match_prog(J) : 0;
+    // compile-time programs: n <= 8 in both precisions, n = 9 (shuffle level) in FP32
+    const bool prog_n = (J.n >= 1 && J.n <= 8) || (J.n == 9 && std::is_same<real, float>::value);
+    const int prog = (!pout && prog_n && fast_levels_ok(J)) ? match_prog(J) : 0;
     if (prog) {
         switch (J.n) {
             case 1: return launch_prog<real, 1>(J, tw, total, prog, st);
@@ -775,6 +825,9 @@ static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double
             case 6: return launch_prog<real, 6>(J, tw, total, prog, st);
             case 7: return launch_prog<real, 7>(J, tw, total, prog, st);
             case 8: return launch_prog<real, 8>(J, tw, total, prog, st);
+            case 9:
+                if constexpr (std::is_same<real, float>::value) return launch_prog<real, 9>(J, tw, total, prog, st);
+                break;
         }
     }
     if (fast_ok(J)) {

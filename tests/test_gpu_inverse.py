@@ -108,6 +108,18 @@ def test_n256_hybrid_fp32_vs_cpu_reference_engine(pkg, hybrid256):
     assert rel_err(xg, x) < 0.05  # noisy data: close to the phantom
 
 
+def test_n512_hybrid_fp32_vs_cpu_reference_engine(pkg):
+    """N=512 (row programs with the warp-shuffle level), p=32, dense_cap 16, FP32: <= 1e-5 vs the FP64 C++-engine
+    path on the same plan."""
+    n, N = 9, 512
+    H = pkg.FastHybridGpu(n, deg_cap=32, dense_cap=16, precision="fp32")
+    x = pkg.phantoms.ellipse_phantom(N, seed=17)
+    b = pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, x), 1e-3, seed=18)
+    ref = CE.hybrid_cpu(n, dict(lam_max=H.lam_max, deg=H.deg, dense_cap=16, outer=(H.lo, H.hi, H.outer_deg)),
+                        threads=16).apply(b)
+    assert rel_err(H.apply(b), ref) < 1e-5
+
+
 def test_n256_fp32_without_dense_rows_precision(pkg):
     """Without the dense table the FP32 polynomial filter on the low-frequency rows limits the accuracy: recorded
     here (not hidden) so that a regression in the FP32 path shows."""
