@@ -1,9 +1,9 @@
 // Row engine: per offset-frequency row, the butterflies B_m (levels lo..hi), their adjoints and the fused Chebyshev
 // filter z = p_k(M) y, M = B^* B (reference: cpp/oblique.cpp:22-104, fastops.RowEngine fastops.py:70-138).
 //
-// Fast kernel (n <= 8; the compile-time programs also n = 9 in FP32). A row of N = 2^n complex values is held in
-// registers by a group of T = 2^(n-r) lanes, each holding R = 2^r values, r = ceil(n/2) (r = 4 at n = 9, where the
-// one index bit neither layout holds in registers, bit 4, is a warp-shuffle level). Butterflies run in place: level m pairs the values whose physical index
+// Fast kernel (n <= 8; the compile-time programs also n = 9..11 in FP32). A row of N = 2^n complex values is held in
+// registers by a group of T = 2^(n-r) lanes, each holding R = 2^r values, r = ceil(n/2) (r = 4 from n = 9 on, where
+// a row spans 1, 2 or 4 warps and the index bits neither layout holds in registers, 4..n-5, are warp-shuffle levels). Butterflies run in place: level m pairs the values whose physical index
 // differs in bit m-1, with twiddles z^t, z^(t+1), t = bitrev_{m-1}(p mod 2^(m-1)); in-place forward levels leave the
 // row in bit-reversed order and the adjoint levels restore it, so an M = B^* B application needs no permutation.
 // Two register layouts cover the index bits:
@@ -36,20 +36,26 @@ template <typename real> struct TwSrc {
 
 template <int n> struct FastCfg {
     static constexpr int N = 1 << n;
-    // register bits r = ceil(n/2) up to n = 8; n = 9 keeps 16 values per lane (a whole warp per row), so index bit 4
-    // is held by neither layout's registers and runs as a warp-shuffle level in the A layout (lane u ^ 1)
-    static constexpr int r = n == 9 ? 4 : (n + 1) / 2;
+    // register bits r = ceil(n/2) up to n = 8; from n = 9 on a lane keeps 16 values and a row spans T = 2^(n-4)
+    // lanes (1, 2, 4 warps at n = 9, 10, 11), so index bits 4..n-5 are held by neither layout's registers: they run
+    // as warp-shuffle levels in the A layout (bit 4 + s is lane bit s, partner lane u ^ 2^s)
+    static constexpr int r = n >= 9 ? 4 : (n + 1) / 2;
     static constexpr int R = 1 << r;
     static constexpr int tb = n - r;
     static constexpr int T = 1 << tb;
+    static constexpr int WPG = T > 32 ? T / 32 : 1;  // warps per row group (named barrier when > 1)
     static constexpr int BLO = imax(r, tb);  // the B layout's registers hold index bits BLO..n-1
     static constexpr int MID = BLO - r;      // shuffle levels r+1..BLO
-    static_assert(T <= 32 && MID <= 1, "row group must fit one warp, with at most one shuffle level");
+    static_assert(MID <= 3 && (MID == 0 || r + MID <= r + 5), "shuffle levels must stay within a warp's lane bits");
+    // per-row table z^0..z^(2^(BLO-1)) in shared memory for the lane-dependent shuffle-level twiddles (MID >= 2)
+    static constexpr int ZT = MID >= 2 ? (1 << (BLO - 1)) + 1 : 0;
     static constexpr int NB = (n > BLO) ? ((1 << (BLO - tb)) * ((1 << (n - BLO)) - 1)) : 0;
     static constexpr int SW_SHIFT = imax(r, 4);
     static constexpr int SW_MASK = (1 << imin(r - 1, 3)) - 1;
     static constexpr int PAD = (T < 16) ? 8 : 0;
     static constexpr int BUF = N + PAD;
+    // shared memory of one row group in complex elements: exchange buffer, filter input, twiddle table, work slot
+    static constexpr int GS = BUF + N + ((ZT + 1) & ~1) + (WPG > 1 ? 2 : 0);
     __host__ __device__ static constexpr int phys(int p) { return p ^ (((p >> SW_SHIFT) & SW_MASK) << 1); }
     __host__ __device__ static constexpr int offB(int b) { return (1 << (BLO - tb)) * ((1 << (b - BLO)) - 1); }
 };
@@ -144,34 +150,64 @@ template <typename C, int n> struct Lanes {
     __device__ __forceinline__ static C twx(const C (&tA)[R / 2 + 1], int t) {
         return t <= R / 2 ? tA[t] : cmul(tA[R / 2], tA[t - R / 2]);
     }
-    // the shuffle level (index bit r, level r+1) in the A layout, p = j + R u: the pair partner of slot j is slot j
-    // of lane u ^ 1, and the twiddle index t = bitrev_r(j) is the same in every lane
-    __device__ __forceinline__ static void fwdM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u) {
-        if (F::MID && r + 1 >= lo && r + 1 <= hi) {
-            const bool upper = u & 1;
+    // the shuffle levels (index bits r + s, s < MID) in the A layout, p = j + R u: the pair partner of slot j is slot j
+    // of lane u ^ 2^s, and the twiddle index is t = bitrev_(r+s)(p mod 2^(r+s)) = bitrev_r(j) 2^s + bitrev_s(u mod 2^s)
+    // (the same in every lane for s = 0; from the per-row table zt otherwise)
+    __device__ __forceinline__ static void mid_tw(const C (&tA)[R / 2 + 1], const C* zt, int s, int j, int ul, C& za,
+                                                  C& zb) {
+        if (s == 0) {
+            za = twx(tA, brev(j, r));
+            zb = twx(tA, brev(j, r) + 1);
+        } else {
+            const int t = (brev(j, r) << s) | ul;
+            za = zt[t];
+            zb = zt[t + 1];
+        }
+    }
+    __device__ __forceinline__ static void fwdM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u,
+                                                const C* zt = nullptr) {
 #pragma unroll
-            for (int j = 0; j < R; ++j) {
-                const int t = brev(j, r);
-                C o;
-                o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1);
-                o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1);
-                const C f0 = upper ? o : v[j], f1 = upper ? v[j] : o;
-                v[j] = cfma(upper ? twx(tA, t + 1) : twx(tA, t), f1, f0);
+        for (int s = 0; s < F::MID; ++s) {
+            if (r + s + 1 >= lo && r + s + 1 <= hi) {
+                const bool upper = (u >> s) & 1;
+                const int ul = s ? (int)(__brev((unsigned)(u & ((1 << s) - 1))) >> (32 - (s ? s : 1))) : 0;
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    C o, za, zb;
+                    o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1 << s);
+                    o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1 << s);
+                    mid_tw(tA, zt, s, j, ul, za, zb);
+                    const C f0 = upper ? o : v[j], f1 = upper ? v[j] : o;
+                    v[j] = cfma(upper ? zb : za, f1, f0);
+                }
             }
         }
     }
-    __device__ __forceinline__ static void adjM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u) {
-        if (F::MID && r + 1 >= lo && r + 1 <= hi) {
-            const bool upper = u & 1;
+    __device__ __forceinline__ static void adjM(C (&v)[R], const C (&tA)[R / 2 + 1], int lo, int hi, int u,
+                                                const C* zt = nullptr) {
 #pragma unroll
-            for (int j = 0; j < R; ++j) {
-                const int t = brev(j, r);
-                C o;
-                o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1);
-                o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1);
-                const C g0 = upper ? o : v[j], g1 = upper ? v[j] : o;
-                v[j] = upper ? cdot2c(twx(tA, t), g0, twx(tA, t + 1), g1) : cadd(g0, g1);
+        for (int s = F::MID - 1; s >= 0; --s) {
+            if (r + s + 1 >= lo && r + s + 1 <= hi) {
+                const bool upper = (u >> s) & 1;
+                const int ul = s ? (int)(__brev((unsigned)(u & ((1 << s) - 1))) >> (32 - (s ? s : 1))) : 0;
+#pragma unroll
+                for (int j = 0; j < R; ++j) {
+                    C o, za, zb;
+                    o.x = __shfl_xor_sync(0xffffffffu, v[j].x, 1 << s);
+                    o.y = __shfl_xor_sync(0xffffffffu, v[j].y, 1 << s);
+                    mid_tw(tA, zt, s, j, ul, za, zb);
+                    const C g0 = upper ? o : v[j], g1 = upper ? v[j] : o;
+                    v[j] = upper ? cdot2c(za, g0, zb, g1) : cadd(g0, g1);
+                }
             }
+        }
+    }
+    // barrier of one row group: the warp's lanes, or a named barrier over the group's warps
+    __device__ __forceinline__ static void gsync(unsigned gmask) {
+        if (F::WPG > 1) {
+            asm volatile("bar.sync %0, %1;" ::"r"(1 + (int)(threadIdx.x / T)), "r"(T) : "memory");
+        } else {
+            __syncwarp(gmask);
         }
     }
     // A layout -> B layout through the group's buffer
@@ -180,49 +216,52 @@ template <typename C, int n> struct Lanes {
 #pragma unroll
             for (int j = 0; j < R; j += 2) st2(buf + F::phys(j + R * u), v[j], v[j + 1]);
         }
-        __syncwarp(gmask);
+        gsync(gmask);
 #pragma unroll
         for (int j = 0; j < R; ++j) v[j] = buf[F::phys(u + T * j)];
-        __syncwarp(gmask);
+        gsync(gmask);
     }
     __device__ __forceinline__ static void toA(C (&v)[R], C* buf, int u, unsigned gmask) {
 #pragma unroll
         for (int j = 0; j < R; ++j) buf[F::phys(u + T * j)] = v[j];
-        __syncwarp(gmask);
+        gsync(gmask);
 #pragma unroll
         for (int j = 0; j < R; j += 2) ld2(buf + F::phys(j + R * u), v[j], v[j + 1]);
-        __syncwarp(gmask);
+        gsync(gmask);
     }
     __device__ __forceinline__ static void fwd(C (&v)[R], const C (&tA)[R / 2 + 1], const C (&t0)[NB ? NB : 1],
-                                               const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm) {
+                                               const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm,
+                                               const C* zt = nullptr) {
         fwdA(v, tA, lo, hi);
         if (hi > r) {
-            fwdM(v, tA, lo, hi, u);
+            fwdM(v, tA, lo, hi, u, zt);
             toB(v, buf, u, gm);
             fwdB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
         }
     }
     __device__ __forceinline__ static void adj(C (&v)[R], const C (&tA)[R / 2 + 1], const C (&t0)[NB ? NB : 1],
-                                               const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm) {
+                                               const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm,
+                                               const C* zt = nullptr) {
         if (hi > r) {
             toB(v, buf, u, gm);
             adjB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
-            adjM(v, tA, lo, hi, u);
+            adjM(v, tA, lo, hi, u, zt);
         }
         adjA(v, tA, lo, hi);
     }
     __device__ __forceinline__ static void gram(C (&v)[R], const C (&tA)[R / 2 + 1], const C (&t0)[NB ? NB : 1],
-                                                const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm) {
+                                                const C (&t1)[NB ? NB : 1], int lo, int hi, C* buf, int u, unsigned gm,
+                                               const C* zt = nullptr) {
         fwdA(v, tA, lo, hi);
         if (hi > r) {
-            fwdM(v, tA, lo, hi, u);
+            fwdM(v, tA, lo, hi, u, zt);
             toB(v, buf, u, gm);
             fwdB(v, t0, t1, lo, hi);
             adjB(v, t0, t1, lo, hi);
             toA(v, buf, u, gm);
-            adjM(v, tA, lo, hi, u);
+            adjM(v, tA, lo, hi, u, zt);
         }
         adjA(v, tA, lo, hi);
     }
@@ -237,7 +276,7 @@ __global__ void __launch_bounds__(THREADS, 1)
     using C = cplx<real>;
     using F = FastCfg<n>;
     using Ln = Lanes<C, n>;
-    constexpr int N = F::N, r = F::r, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
+    constexpr int N = F::N, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
     constexpr int GPW = 32 / T;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
@@ -398,7 +437,7 @@ template <typename C, int n> struct CtLanes {
     template <int LO, int HI>
     __device__ __forceinline__ static void fwd_oop(const C (&src)[R], C (&dst)[R], const C (&tA)[R / 2 + 1],
                                                    const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], C* buf, int u,
-                                                   unsigned gm) {
+                                                   unsigned gm, const C* zt) {
 #pragma unroll
         for (int b = 0; b < r; ++b) {
             if (b + 1 >= LO && b + 1 <= HI) {
@@ -414,7 +453,7 @@ template <typename C, int n> struct CtLanes {
             }
         }
         if (HI > r) {
-            Ln::fwdM(dst, tA, LO, HI, u);
+            Ln::fwdM(dst, tA, LO, HI, u, zt);
             Ln::toB(dst, buf, u, gm);
             Ln::fwdB(dst, t0, t1, LO, HI);
         }
@@ -423,12 +462,12 @@ template <typename C, int n> struct CtLanes {
     template <int LO, int HI>
     __device__ __forceinline__ static void gram_oop(const C (&src)[R], C (&dst)[R], const C (&tA)[R / 2 + 1],
                                                     const C (&t0)[NB ? NB : 1], const C (&t1)[NB ? NB : 1], C* buf,
-                                                    int u, unsigned gm) {
-        fwd_oop<LO, HI>(src, dst, tA, t0, t1, buf, u, gm);
+                                                    int u, unsigned gm, const C* zt) {
+        fwd_oop<LO, HI>(src, dst, tA, t0, t1, buf, u, gm, zt);
         if (HI > r) {
             Ln::adjB(dst, t0, t1, LO, HI);
             Ln::toA(dst, buf, u, gm);
-            Ln::adjM(dst, tA, LO, HI, u);
+            Ln::adjM(dst, tA, LO, HI, u, zt);
         }
         Ln::adjA(dst, tA, LO, HI);
     }
@@ -441,29 +480,43 @@ __global__ void __launch_bounds__(THREADS, 1)
     using F = FastCfg<n>;
     using Ln = Lanes<C, n>;
     using Ct = CtLanes<C, n>;
-    constexpr int N = F::N, r = F::r, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
+    constexpr int N = F::N, R = F::R, T = F::T, tb = F::tb, NB = F::NB;
     constexpr int GPW = 32 / T;
     constexpr bool HYB = (PROG == PROG_GH_HYB || PROG == PROG_BP_HYB);
     constexpr int LO = HYB ? 2 : 1;  // filter levels LO..n
     constexpr bool BP = (PROG == PROG_BP_HYB || PROG == PROG_BP_LP);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
-    const int giw = lane / T;
-    const int u = lane & (T - 1);
-    C* buf = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / T) * (F::BUF + F::N);
+    const int giw = T >= 32 ? 0 : lane / T;
+    const int u = threadIdx.x & (T - 1);
+    C* buf = reinterpret_cast<C*>(smem_raw) + (threadIdx.x / T) * F::GS;
     C* ybuf = buf + F::BUF;
-    const unsigned gm = (T == 32) ? 0xffffffffu : (((1u << T) - 1u) << (giw * T));
+    C* zt = ybuf + F::N;  // shuffle-level twiddles (MID >= 2)
+    int* slot = reinterpret_cast<int*>(zt + ((F::ZT + 1) & ~1));  // the group's work item (WPG > 1)
+    const unsigned gm = (T >= 32) ? 0xffffffffu : (((1u << T) - 1u) << (giw * T));
     C* X = reinterpret_cast<C*>(J.X);
     const real tau = (real)J.tau;
     const real* coefs = reinterpret_cast<const real*>(J.coef);
 
     for (;;) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(J.counter, GPW);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= total) break;
-        const bool last = base + GPW >= total;
-        const int item = base + giw;
+        int item = 0;
+        bool last = false;
+        if (F::WPG > 1) {
+            // a row spans several warps: the group's first thread takes the item, a named barrier shares it (the
+            // second barrier keeps the slot until every warp of the group has read it)
+            if (u == 0) *slot = atomicAdd(J.counter, 1);
+            Ln::gsync(gm);
+            item = *slot;
+            Ln::gsync(gm);
+            if (item >= total) break;
+        } else {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(J.counter, GPW);
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (base >= total) break;
+            last = base + GPW >= total;
+            item = base + giw;
+        }
         if (item < total) {
             const int sel = item / J.nimg;
             const int img = item - sel * J.nimg;
@@ -493,12 +546,18 @@ __global__ void __launch_bounds__(THREADS, 1)
                 }
             }
 
+            if (F::ZT) {
+#pragma unroll 1
+                for (int t = u; t < F::ZT; t += T) zt[t] = tw.get(key, t);
+                Ln::gsync(gm);
+            }
+
             C v[R], w[R], dl[R];
             if (BP) {
                 // the back-projections start with the adjoint levels LO..n on rows in natural (slope) order
 #pragma unroll
                 for (int j = 0; j < R; ++j) v[j] = ptr[bfly_perm(j + R * u, n)];
-                Ln::adj(v, tA, t0, t1, LO, n, buf, u, gm);
+                Ln::adj(v, tA, t0, t1, LO, n, buf, u, gm, zt);
             } else {
 #pragma unroll
                 for (int j = 0; j < R; j += 2) ld2(ptr + j + R * u, v[j], v[j + 1]);
@@ -517,7 +576,7 @@ __global__ void __launch_bounds__(THREADS, 1)
             real om_a = d > 1 ? cf[2] : (real)0, om_1 = d > 1 ? cf[3] : (real)0;  // step 1
             for (int s = 1; s <= steps; ++s) {
                 const real na = (s + 1 < d) ? cf[3 * s + 2] : (real)0, n1 = (s + 1 < d) ? cf[3 * s + 3] : (real)0;
-                Ct::template gram_oop<LO, n>(v, w, tA, t0, t1, buf, u, gm);
+                Ct::template gram_oop<LO, n>(v, w, tA, t0, t1, buf, u, gm, zt);
                 if (s == d) break;  // w = M z_d
 #pragma unroll
                 for (int j = 0; j < R; j += 2) {
@@ -726,7 +785,7 @@ template <typename real, int n>
 static int launch_fast(const adrt_row_job& J, const TwSrc<real>& tw, int total, int iters, double safety, double* pout,
                        cudaStream_t st) {
     using F = FastCfg<n>;
-    const size_t smem = (size_t)(FAST_THREADS / F::T) * (F::BUF + F::N) * sizeof(cplx<real>);
+    const size_t smem = (size_t)(FAST_THREADS / F::T) * F::GS * sizeof(cplx<real>);
     auto kern = pout ? rows_fast_kernel<real, n, FAST_THREADS, true> : rows_fast_kernel<real, n, FAST_THREADS, false>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     const int grid = J.grid > 0 ? J.grid : num_sms();
@@ -770,7 +829,7 @@ static bool fast_ok(const adrt_row_job& J) { return J.n >= 1 && J.n <= 8 && fast
 template <typename real, int n>
 static int launch_prog(const adrt_row_job& J, const TwSrc<real>& tw, int total, int prog, cudaStream_t st) {
     using F = FastCfg<n>;
-    const size_t smem = (size_t)(FAST_THREADS / F::T) * (F::BUF + F::N) * sizeof(cplx<real>);
+    const size_t smem = (size_t)(FAST_THREADS / F::T) * F::GS * sizeof(cplx<real>);
     void (*kern)(const adrt_row_job, const TwSrc<real>, const int) = nullptr;
     switch (prog) {
         case PROG_GH_HYB: kern = rows_prog_kernel<real, n, FAST_THREADS, PROG_GH_HYB>; break;
@@ -812,8 +871,8 @@ static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double
         return ADRT_EINVAL;
     }
     const int total = (int)total_l;
-    // compile-time programs: n <= 8 in both precisions, n = 9 (shuffle level) in FP32
-    const bool prog_n = (J.n >= 1 && J.n <= 8) || (J.n == 9 && std::is_same<real, float>::value);
+    // compile-time programs: n <= 8 in both precisions, n = 9..11 (shuffle levels) in FP32
+    const bool prog_n = (J.n >= 1 && J.n <= 8) || (J.n <= 11 && std::is_same<real, float>::value);
     const int prog = (!pout && prog_n && fast_levels_ok(J)) ? match_prog(J) : 0;
     if (prog) {
         switch (J.n) {
@@ -827,6 +886,12 @@ static int rows_dispatch(const adrt_row_job& J, int iters, double safety, double
             case 8: return launch_prog<real, 8>(J, tw, total, prog, st);
             case 9:
                 if constexpr (std::is_same<real, float>::value) return launch_prog<real, 9>(J, tw, total, prog, st);
+                break;
+            case 10:
+                if constexpr (std::is_same<real, float>::value) return launch_prog<real, 10>(J, tw, total, prog, st);
+                break;
+            case 11:
+                if constexpr (std::is_same<real, float>::value) return launch_prog<real, 11>(J, tw, total, prog, st);
                 break;
         }
     }

@@ -125,25 +125,27 @@ def test_device_rows_fp32(pkg, n, tol):
     assert max_rel(out, ref) < tol
 
 
+@pytest.mark.parametrize("n", [9, 10, 11])
 @pytest.mark.parametrize("name", ["lp", "hyb"])
-def test_device_programs_fp32_n9(pkg, name):
-    """The compile-time row programs at n = 9 (16 values per lane, one warp per row, index bit 4 as a warp-shuffle
-    level) on all four packed op lists against the FP64 oracle. Degrees capped at 6 keep the polynomial's FP32
-    error amplification small, so the tolerance checks the index arithmetic rather than the conditioning."""
+def test_device_programs_fp32_large_n(pkg, name, n):
+    """The compile-time row programs at n = 9..11 (16 values per lane, rows over 1, 2, 4 warps, index bits 4..n-5 as
+    warp-shuffle levels, named barriers per row group) on all four packed op lists against the FP64 oracle. Degrees
+    capped at 6 keep the polynomial's FP32 error amplification small, so the tolerance checks the index arithmetic
+    rather than the conditioning."""
     import torch
 
-    n = 9
     N, L = 1 << n, 2 << n
+    nimg = 2 if n < 11 else 1
     lo = 1 if name == "lp" else 2
     lam = O.power_lam_max(n, O.offset_z(L), lo, iters=10)
     plan = pkg.Plan("lp" if name == "lp" else "hybrid", n, lam, deg_cap=6)
     tabs = pkg.device.RowTables(plan, torch.float32, torch.device("cuda"))
     ref_eng = O.RowEngineOracle(n, O.offset_z(L), plan.deg, plan.lam_max, plan.tau, 2, None, (lo, None))
     rng = np.random.default_rng(9)
-    Y = rng.standard_normal((2, 2 * L, N)) + 1j * rng.standard_normal((2, 2 * L, N))
+    Y = rng.standard_normal((nimg, 2 * L, N)) + 1j * rng.standard_normal((nimg, 2 * L, N))
     for ops in PACKED[name](n):
         Yd = torch.from_numpy(Y).to("cuda", torch.complex64).contiguous()
         tabs.run(Yd, ops)
         out = Yd.cpu().numpy()
-        for i in range(2):
+        for i in range(nimg):
             assert max_rel(out[i], ref_eng.run(Y[i], ops)) < 5e-6, (ops, i)
