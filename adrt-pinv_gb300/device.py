@@ -107,11 +107,22 @@ class RowTables:
         return tot
 
     def dense_table(self, fold_pre, fold_post, pre_b1=False, post_b1t=False):
+        """The folded dense-row operators of one op list, one per dense packed row, in the row precision. Built on
+        the host in FP64 up to n = 8 and on the device (FP64 torch, Cholesky form) for larger n."""
         key = (fold_pre, fold_post, pre_b1, post_b1t)
         if key not in self._dense_dev:
-            T = self.plan.dense_row_operator(fold_pre, fold_post, pre_b1, post_b1t)
-            self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T[self.dense_sel])).to(
-                device=self.device, dtype=_cdtype(self.real))
+            if self.plan.n >= 9 and self.device.type == "cuda":
+                N = self.plan.N
+                out = torch.empty((len(self.dense_sel), N, N), dtype=_cdtype(self.real), device=self.device)
+                sel = torch.from_numpy(self.dense_sel).to(self.device)
+                for c0, T in dense_row_operator_device(self.plan, fold_pre, fold_post, pre_b1, post_b1t, self.device):
+                    hit = ((sel >= c0) & (sel < c0 + T.shape[0])).nonzero().flatten()
+                    out[hit] = T[sel[hit] - c0].to(out.dtype)
+                self._dense_dev[key] = out
+            else:
+                T = self.plan.dense_row_operator(fold_pre, fold_post, pre_b1, post_b1t)
+                self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T[self.dense_sel])).to(
+                    device=self.device, dtype=_cdtype(self.real))
         return self._dense_dev[key]
 
     def dense_apply(self, Y, T):
@@ -165,6 +176,70 @@ class RowTables:
             if post:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, post, self.rows_dense)), st)
         self.count += B * self.plan.level_rows(ops_unfused(ops))
+
+
+def _rows_apply_f64(X, z_rows, ops, n, counter):
+    """The row ops on the K rows of X (K, N) complex128 in place (natural order in and out), row i at frequency
+    z_rows[i] (complex128 on the device), through the library's FP64 row kernels with a per-row twiddle table."""
+    K, N = X.shape
+    st = C.stream_handle()
+    tab = torch.empty((K, N // 2 + 1), dtype=torch.complex128, device=X.device)
+    C.call("adrt_twiddle_table", C.dtype_code(torch.float64), n, K, C.ptr(z_rows), C.ptr(tab), st)
+    j = C.RowJob()
+    j.dtype, j.n, j.nimg, j.nsel, j.img_stride = C.dtype_code(torch.float64), n, 1, K, K * N
+    j.X, j.rows, j.freq_mod, j.roots, j.twtab = X.data_ptr(), None, K, None, tab.data_ptr()
+    j.deg, j.coef, j.coef_stride, j.tau = None, None, 0, 0.0
+    j.nops = len(ops)
+    for i, (op, lo, hi) in enumerate(ops):
+        j.op[i], j.lo[i], j.hi[i] = OPCODE[op], lo, hi
+    j.counter, j.grid = counter.data_ptr(), 0
+    C.call("adrt_rows_run", ctypes.byref(j), st)
+
+
+def dense_row_operator_device(plan: Plan, fold_pre, fold_post, pre_b1, post_b1t, device, chunk=None):
+    """Plan.dense_row_operator built on the device in FP64, in chunks of dense frequencies: yields (first index,
+    (k, N, N) complex128). The Gram matrices M_k and every butterfly fold come from the library's own FP64 row
+    kernels applied to unit vectors (O(n N^2) per frequency instead of a dense O(N^3) product):
+        rows of M e_j          -> M^T = conj(M)                    (M Hermitian)
+        T A^H,  row t          -> conj(A conj(t))                  (A = B_hi ... B_lo)
+        T B_1,  row t          -> conj(B_1^* conj(t))
+        B_1^* T                -> B_1^* applied to the columns of T
+    and the filter itself from one Cholesky factorisation and inverse per frequency (torch, FP64):
+        F = (M + tau I)^-1,   M F = I - tau F."""
+    n, N, Kd, tau = plan.n, plan.N, len(plan.dense_freqs), plan.tau
+    lo, hi = plan.p_levels
+    dev = torch.device(device)
+    z = torch.from_numpy(roots_of_unity(plan.L)[plan.dense_freqs]).to(dev)
+    if chunk is None:
+        chunk = max(1, min(Kd, (1 << 29) // (N * N * 16)))  # about 512 MB per (k, N, N) block
+    eye = torch.eye(N, dtype=torch.complex128, device=dev)
+    counter = torch.zeros(4, dtype=torch.int32, device=dev)
+    for c0 in range(0, Kd, chunk):
+        zc = z[c0:c0 + chunk]
+        k = zc.shape[0]
+        zr = zc.repeat_interleave(N)
+        # the kernels read raw memory: every conjugate handed to them is materialised (conj_physical, not the
+        # lazy conjugate view)
+        X = eye.expand(k, N, N).reshape(k * N, N).clone()
+        _rows_apply_f64(X, zr, [("M", lo, hi)], n, counter)
+        Mk = torch.conj_physical(X.view(k, N, N))
+        Mk.diagonal(dim1=-2, dim2=-1).add_(tau)
+        F = torch.cholesky_inverse(torch.linalg.cholesky(Mk))
+        del Mk, X
+        T = eye - tau * F if fold_post else F
+        if fold_pre:
+            X = torch.conj_physical(T).reshape(k * N, N).contiguous()
+            _rows_apply_f64(X, zr, [("B", lo, hi)], n, counter)
+            T = torch.conj_physical(X.view(k, N, N))
+        if pre_b1:
+            X = torch.conj_physical(T).reshape(k * N, N).contiguous()
+            _rows_apply_f64(X, zr, [("BT", 1, 1)], n, counter)
+            T = torch.conj_physical(X.view(k, N, N))
+        if post_b1t:
+            X = T.transpose(-1, -2).reshape(k * N, N).contiguous()
+            _rows_apply_f64(X, zr, [("BT", 1, 1)], n, counter)
+            T = X.view(k, N, N).transpose(-1, -2)
+        yield c0, T
 
 
 def ops_unfused(ops):

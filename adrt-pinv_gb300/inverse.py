@@ -125,7 +125,9 @@ class _GpuInverse:
         import scipy.sparse.linalg as spla
 
         N = self.N
-        pipe = self.pipeline(1, "fp64")
+        # the interval is estimated to a relative accuracy of about 1e-3 and widened by 1% on both sides: the FP64
+        # operator is used up to N = 512, the FP32 one (relative error ~1e-6) above, where FP64 matvecs dominate setup
+        pipe = self.pipeline(1, "fp64" if N <= 512 else "fp32")
 
         def G(v):
             return self._image_op(pipe, lambda x: pipe.G(x), v.reshape(N, N)).ravel()

@@ -212,6 +212,51 @@ class Plan:
         cache[key] = np.array(mats) if mats else None
         return cache[key]
 
+    def dense_row_operator_torch(self, fold_pre_adjoint, fold_post_gram, pre_b1, post_b1t, device, chunk=None):
+        """dense_row_operator computed with torch on `device` (batched over chunks of dense frequencies), FP64,
+        returned as a (Kd, N, N) complex128 tensor on that device. Instead of an eigendecomposition it uses the
+        identities F = (M + tau I)^-1 (one Cholesky factorisation and inverse per frequency) and
+        M F = I - tau F, exact in exact arithmetic and about five times cheaper; used for large N, where the host
+        eigendecompositions dominate the setup."""
+        import torch
+
+        Kd = len(self.dense_freqs)
+        if not Kd:
+            return None
+        out = torch.empty((Kd, self.N, self.N), dtype=torch.complex128, device=torch.device(device))
+        for c0, T in self.dense_row_operator_chunks(fold_pre_adjoint, fold_post_gram, pre_b1, post_b1t, device, chunk):
+            out[c0:c0 + T.shape[0]] = T
+        return out
+
+    def dense_row_operator_chunks(self, fold_pre_adjoint, fold_post_gram, pre_b1, post_b1t, device, chunk=None):
+        """The chunks (first dense-frequency index, (k, N, N) complex128 tensor) of dense_row_operator_torch."""
+        import torch
+
+        n, N, Kd = self.n, self.N, len(self.dense_freqs)
+        lo, hi = self.p_levels
+        dev = torch.device(device)
+        z = torch.from_numpy(roots_of_unity(self.L)[self.dense_freqs]).to(dev)
+        if chunk is None:
+            chunk = max(1, min(Kd, (1 << 30) // (N * N * 16)))  # about 1 GB per N x N batch
+        eye = torch.eye(N, dtype=torch.complex128, device=dev)
+        for c0 in range(0, Kd, chunk):
+            zc = z[c0:c0 + chunk]
+            A = _butterfly_matrix_torch(n, zc, lo, hi)
+            F = A.mH @ A
+            F.diagonal(dim1=-2, dim2=-1).add_(self.tau)
+            F = torch.cholesky_inverse(torch.linalg.cholesky(F))
+            T = eye - self.tau * F if fold_post_gram else F
+            if fold_pre_adjoint:
+                T = T @ A.mH
+            del A, F
+            if pre_b1 or post_b1t:
+                B1 = _butterfly_matrix_torch(n, zc, 1, 1)
+                if pre_b1:
+                    T = T @ B1
+                if post_b1t:
+                    T = B1.mH @ T
+            yield c0, T
+
     # ---------------------------------------------------------------- cache
     def save(self, path):
         np.savez(path, method=self.method, n=self.n, lam_max=self.lam_max, tau_fac=self.tau_fac, eps_in=self.eps_in,
@@ -243,3 +288,22 @@ def _butterfly_matrix(n, zk, lo, hi):
         out[..., 1] = src[:, :, 0, :] + u * zk
         X = out.reshape(N, N)
     return X.T
+
+
+def _butterfly_matrix_torch(n, zk, lo, hi):
+    """_butterfly_matrix for a batch of frequencies zk (k,) with torch: (k, N, N) complex128 on zk's device."""
+    import torch
+
+    N = 1 << n
+    k = zk.shape[0]
+    X = torch.eye(N, dtype=torch.complex128, device=zk.device).expand(k, N, N).contiguous()
+    for m in range(lo, hi + 1):
+        w = 1 << (m - 1)
+        src = X.reshape(k, N, N // (2 * w), 2, w)
+        tw = zk[:, None] ** torch.arange(w, device=zk.device, dtype=torch.float64)[None, :]
+        u = src[:, :, :, 1, :] * tw[:, None, None, :]
+        out = torch.empty((k, N, N // (2 * w), w, 2), dtype=torch.complex128, device=zk.device)
+        out[..., 0] = src[:, :, :, 0, :] + u
+        out[..., 1] = src[:, :, :, 0, :] + u * zk[:, None, None, None]
+        X = out.reshape(k, N, N)
+    return X.transpose(-1, -2)

@@ -76,10 +76,11 @@ class Lane:
     def done(self):
         return self.batch is not None and self.event.query()
 
-    def collect(self):
+    def collect(self, keep=None):
+        """The finished batch; each request's result is copied out of the staging buffer unless keep(r) is false."""
         out = self.batch
         for i, r in enumerate(out):
-            r.result = self.stage_out[i].clone()
+            r.result = self.stage_out[i].clone() if keep is None or keep(r) else None
         self.batch = None
         return out
 
@@ -90,12 +91,14 @@ class Lane:
 
 
 class InverseServer:
-    """make_inverse(n) -> FastHybridGpu / FastLpGpu of size 2^n; slots(n) -> batch slots of that size's lane."""
+    """make_inverse(key) -> FastHybridGpu / FastLpGpu for a request key (its size n, or any hashable class such as
+    (n, method, p)); slots(key) -> batch slots of that key's lane. Request.n holds the key."""
 
     lane_cls = Lane
 
-    def __init__(self, make_inverse, slots, hbm_budget_bytes=120e9, device="cuda"):
+    def __init__(self, make_inverse, slots, hbm_budget_bytes=120e9, device="cuda", keep_result=None):
         self.make_inverse, self.slots, self.budget = make_inverse, slots, float(hbm_budget_bytes)
+        self.keep_result = keep_result  # keep_result(request) -> bool; None keeps every result
         self.device = torch.device(device)
         self.inverses, self.lanes, self.queues, self.last_used = {}, {}, {}, {}
         self.finished = []
@@ -139,7 +142,7 @@ class InverseServer:
         for n, lane in self.lanes.items():
             if lane.done():
                 t = self.clock()
-                for r in lane.collect():
+                for r in lane.collect(self.keep_result):
                     r.t_done = t
                     self.finished.append(r)
         for n, q in self.queues.items():

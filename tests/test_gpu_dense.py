@@ -44,3 +44,21 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
            C.ptr(Zd), None, 0, C.stream_handle())
     torch.cuda.synchronize()
     assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
+
+
+@pytest.mark.parametrize("method", ["hybrid", "lp"])
+def test_device_built_dense_operators_match_host(pkg, method):
+    """Dense-row operators built on the device (FP64 row kernels on unit vectors + Cholesky, used for n >= 9) equal
+    the host eigendecomposition form for every folding."""
+    import numpy as np
+
+    from adrt_pinv_gb300.device import dense_row_operator_device
+    from adrt_pinv_gb300.plan import Plan
+
+    n, N = 6, 64
+    plan = Plan(method, n, np.full(2 * N, 50.0 * N), 0.2, 0.1, 1e-10, dense_cap=8)
+    for key in [(a, b, c, d) for a in (0, 1) for b in (0, 1) for c in (0, 1) for d in (0, 1)]:
+        ref = plan.dense_row_operator(*map(bool, key))
+        got = np.concatenate([T.cpu().numpy() for _, T in
+                              dense_row_operator_device(plan, *map(bool, key), device="cuda", chunk=37)])
+        assert np.abs(got - ref).max() <= 1e-11 * np.abs(ref).max(), key

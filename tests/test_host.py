@@ -155,3 +155,18 @@ def test_phantoms_deterministic(pkg):
     assert t.shape == (32, 32) and np.isfinite(t).all()
     im = ph.int_image(16, 2)
     assert im.dtype == np.int32 and im.min() >= 0 and im.max() <= 255
+
+
+@pytest.mark.parametrize("method", ["hybrid", "lp"])
+def test_dense_operator_torch_matches_host(pkg, method):
+    """The device (torch, Cholesky form) dense-row operators used for n >= 9 equal the host eigendecomposition
+    form for every folding, here with torch on the CPU."""
+    from adrt_pinv_gb300.plan import Plan
+
+    n, N = 5, 32
+    plan = Plan(method, n, np.full(2 * N, 50.0 * N), 0.2, 0.1, 1e-10, dense_cap=8)
+    assert len(plan.dense_freqs) > 0
+    for key in [(a, b, c, d) for a in (0, 1) for b in (0, 1) for c in (0, 1) for d in (0, 1)]:
+        ref = plan.dense_row_operator(*map(bool, key))
+        got = plan.dense_row_operator_torch(*map(bool, key), device="cpu", chunk=5).numpy()
+        assert np.abs(got - ref).max() <= 1e-12 * np.abs(ref).max(), key

@@ -31,7 +31,7 @@ class FakeLane:
     def done(self):
         return self.batch is not None
 
-    def collect(self):
+    def collect(self, keep=None):
         out, self.batch = self.batch, None
         for r in out:
             r.result = ("x", r.rid, self.inv.n)
