@@ -125,6 +125,14 @@ class RowTables:
                     device=self.device, dtype=_cdtype(self.real))
         return self._dense_dev[key]
 
+    def raise_if_error(self):
+        """Raise if a tensor-core dense-row launch gave up on a bounded wait since the last check (reads one int: a
+        device synchronisation, so callers make it where they synchronise anyway); clears the flag."""
+        if int(self.err.item()):
+            self.err.zero_()
+            raise RuntimeError("dense_tc_kernel: an mbarrier wait ran out; the dense-row results of that launch "
+                               "were not written")
+
     def dense_apply(self, Y, T):
         """Y[b, r] <- T_r Y[b, r] for the dense rows (tensor cores in FP32, CUDA cores in FP64)."""
         B, R, N = Y.shape

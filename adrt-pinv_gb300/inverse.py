@@ -210,10 +210,18 @@ class _GpuInverse:
         x = x[0] if single else x
         if out is not None:
             out.copy_(x, non_blocking=True)
+            if not out.is_cuda:
+                pipe.tables.raise_if_error()
             return out
         if not is_torch:
-            return x.cpu().numpy()
-        return x.to("cpu") if host_in else x.clone()
+            res = x.cpu().numpy()
+            pipe.tables.raise_if_error()
+            return res
+        if host_in:
+            res = x.to("cpu")
+            pipe.tables.raise_if_error()
+            return res
+        return x.clone()
 
 
 class FastLpGpu(_GpuInverse):
