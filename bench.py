@@ -199,6 +199,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def max_over_ranks(x, world, device):
+    """The slowest rank's time (replicas: the job ends when the last rank ends); a no-op for one process."""
+    import torch
+    import torch.distributed as dist
+
+    if world <= 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(batch_per_rank, world, seconds):
+    """Whole-job reconstructions/s of `world` replicas, each inverting `batch_per_rank` images in `seconds`."""
+    return batch_per_rank * world / seconds
+
+
 def single_image_rates(H, b_dev, steps, torch):
     """Reconstructions/s of one sinogram at a time on the device: eager Pipeline.apply at batch 1 (the plain
     single-image GPU path) and the same apply replayed from a CUDA graph."""
@@ -275,11 +292,8 @@ def run_ours(args):
     launches = (C.load().adrt_launch_count() - l0) // args.steps
     pipe.tables.timer = None
     ms = e0.elapsed_time(e1) / args.steps
-    ms_t = torch.tensor([ms], device=dev)
-    if world > 1:
-        dist.all_reduce(ms_t, op=dist.ReduceOp.MAX)
-    ms = float(ms_t.item())
-    value = B * world / (ms * 1e-3)
+    ms = max_over_ranks(ms, world, dev)
+    value = replica_throughput(B, world, ms * 1e-3)
     # the G_h launches of the polynomial rows (one per outer step): mean duration and algorithmic FLOPs
     from adrt_pinv_gb300.device import fuse_ops
 
@@ -301,10 +315,7 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = (time.perf_counter() - t0) / args.steps
     barrier()
-    e2e_t = torch.tensor([e2e_s], device=dev)
-    if world > 1:
-        dist.all_reduce(e2e_t, op=dist.ReduceOp.MAX)
-    e2e_value = B * world / float(e2e_t.item())
+    e2e_value = replica_throughput(B, world, max_over_ranks(e2e_s, world, dev))
 
     # ---- the plain single-image GPU path (batch 1, eager launches) and the same under a CUDA graph
     single = single_image_rates(H, b_dev, args.steps, torch)
