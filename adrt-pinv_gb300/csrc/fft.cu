@@ -83,12 +83,8 @@ __device__ __forceinline__ void dit_passes(cplx<real> (&x)[FftCfg<l>::E], const 
     }
 }
 
-template <typename real> __device__ __forceinline__ real ldr(const void* p, int dt, size_t i) {
-    return dt == ADRT_F64 ? (real) reinterpret_cast<const double*>(p)[i] : (real) reinterpret_cast<const float*>(p)[i];
-}
-
-template <typename real, int l>
-__global__ void __launch_bounds__(1024) pack_fft_kernel(int nimg, int src_kind, int src_dtype, const void* __restrict__ src,
+template <typename real, int l, typename SRC>
+__global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) pack_fft_kernel(int nimg, int src_kind, const SRC* __restrict__ src,
                                                         cplx<real>* __restrict__ Y, const cplx<real>* __restrict__ roots_g) {
     using F = FftCfg<l>;
     using C = cplx<real>;
@@ -101,43 +97,67 @@ __global__ void __launch_bounds__(1024) pack_fft_kernel(int nimg, int src_kind, 
     const int c0 = blockIdx.x * CB;
     const int pair = blockIdx.y;
     const int img = blockIdx.z;
-    const int nthr = CB * F::TPC;
+    constexpr int nthr = CB * F::TPC;  // L * CB elements per gather = E per thread
     for (int i = threadIdx.x; i < L; i += nthr) roots[i] = roots_g[i];
 
-    // ---- gather the packed strips of columns c0..c0+CB-1 into tile[i][c]
+    // ---- gather the packed strips of columns c0..c0+CB-1 into tile[i][c]; every thread issues its E loads before
+    // its shared-memory stores (E independent loads in flight)
     if (src_kind == 0) {
         const size_t ib = (size_t)img * N * N;
         // column reads: pair 0 imag = x[N-1-i, c] (quadrant II), pair 1 real = x[i, c] (quadrant III)
-        for (int e = threadIdx.x; e < L * CB; e += nthr) {
+        real v[F::E];
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
             const int c = e % CB, i = e / CB;
-            real v = 0;
-            if (i < N) v = (pair == 0) ? ldr<real>(src, src_dtype, ib + (size_t)(N - 1 - i) * N + c0 + c)
-                                       : ldr<real>(src, src_dtype, ib + (size_t)i * N + c0 + c);
-            if (pair == 0) tile[i * CP + c].y = v; else tile[i * CP + c].x = v;
+            v[k] = 0;
+            if (i < N) v[k] = (real)src[ib + (size_t)(pair == 0 ? N - 1 - i : i) * N + c0 + c];
+        }
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int c = e % CB, i = e / CB;
+            if (pair == 0) tile[i * CP + c].y = v[k]; else tile[i * CP + c].x = v[k];
         }
         // row reads: pair 0 real = x[c, N-1-i] (quadrant I), pair 1 imag = x[N-1-c, N-1-i] (quadrant IV)
-        for (int e = threadIdx.x; e < L * CB; e += nthr) {
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
             const int i = e % L, c = e / L;
-            real v = 0;
+            v[k] = 0;
             if (i < N) {
                 const int rowx = (pair == 0) ? (c0 + c) : (N - 1 - c0 - c);
-                v = ldr<real>(src, src_dtype, ib + (size_t)rowx * N + (N - 1 - i));
+                v[k] = (real)src[ib + (size_t)rowx * N + (N - 1 - i)];
             }
-            if (pair == 0) tile[i * CP + c].x = v; else tile[i * CP + c].y = v;
+        }
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int i = e % L, c = e / L;
+            if (pair == 0) tile[i * CP + c].x = v[k]; else tile[i * CP + c].y = v[k];
         }
     } else {
         // iota of the sinogram quadrants qa = 2*pair, qb = 2*pair+1: S[i] = b[i+N-1] (i < N), 0 (i = N), b[i-N-1]
         const size_t H = 2 * (size_t)N - 1;
         const size_t ba = ((size_t)img * 4 + 2 * pair) * H * N, bb = ba + H * N;
-        for (int e = threadIdx.x; e < L * CB; e += nthr) {
+        real va[F::E], vb[F::E];
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
             const int c = e % CB, i = e / CB;
-            C v = mk<real>(0, 0);
+            va[k] = 0;
+            vb[k] = 0;
             if (i != N) {
                 const size_t h = (i < N) ? (size_t)(i + N - 1) : (size_t)(i - N - 1);
-                v.x = ldr<real>(src, src_dtype, ba + h * N + c0 + c);
-                v.y = ldr<real>(src, src_dtype, bb + h * N + c0 + c);
+                va[k] = (real)src[ba + h * N + c0 + c];
+                vb[k] = (real)src[bb + h * N + c0 + c];
             }
-            tile[i * CP + c] = v;
+        }
+#pragma unroll
+        for (int k = 0; k < F::E; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int c = e % CB, i = e / CB;
+            tile[i * CP + c] = mk<real>(va[k], vb[k]);
         }
     }
     __syncthreads();
@@ -211,17 +231,24 @@ template <typename real, int l> static size_t unpack_smem() {
     return ((size_t)(1 << l) + ((size_t)(1 << l) + (size_t)(1 << (l - 1))) * fft_pad(CB)) * sizeof(cplx<real>);
 }
 
-template <typename real, int l>
-static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, cudaStream_t st) {
+template <typename real, int l, typename SRC>
+static int launch_pack_src(int nimg, int src_kind, const void* src, void* Y, const void* roots, cudaStream_t st) {
     constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
     constexpr int N = 1 << (l - 1);
     const size_t smem = pack_smem<real, l>();
-    auto kern = pack_fft_kernel<real, l>;
+    auto kern = pack_fft_kernel<real, l, SRC>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(N / CB, 2, nimg);
-    kern<<<grid, CB * FftCfg<l>::TPC, smem, st>>>(nimg, src_kind, src_dtype, src, reinterpret_cast<cplx<real>*>(Y),
+    kern<<<grid, CB * FftCfg<l>::TPC, smem, st>>>(nimg, src_kind, reinterpret_cast<const SRC*>(src),
+                                                   reinterpret_cast<cplx<real>*>(Y),
                                                    reinterpret_cast<const cplx<real>*>(roots));
     return launch_status("pack_fft_kernel");
+}
+
+template <typename real, int l>
+static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, cudaStream_t st) {
+    if (src_dtype == ADRT_F64) return launch_pack_src<real, l, double>(nimg, src_kind, src, Y, roots, st);
+    return launch_pack_src<real, l, float>(nimg, src_kind, src, Y, roots, st);
 }
 
 template <typename real, int l>
