@@ -190,12 +190,34 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
             promote(s);
         }
         const int i0 = kc * (TC_KC / 2);
-        for (int cm = warp; cm < (TC_M / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
+        // operand tiles: every thread issues all its loads of the chunk first (AIT + XIT independent loads in
+        // flight), then splits and stores them; core matrix cm = warp + it * 8
+        constexpr int AIT = (TC_M / 8) * (TC_KC / 4) / (TC_THREADS / 32);
+        constexpr int XIT = (BP / 8) * (TC_KC / 4) / (TC_THREADS / 32);
+        float2 wv[AIT], yv[XIT];
+#pragma unroll
+        for (int it = 0; it < AIT; ++it) {
+            const int cm = warp + it * (TC_THREADS / 32);
             const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
             const int m = m0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
             const int outhalf = m >= N ? 1 : 0;
-            const float2 w = Wr[(size_t)(m - outhalf * N) * N + i0 + (k >> 1)];
+            wv[it] = Wr[(size_t)(m - outhalf * N) * N + i0 + (k >> 1)];
+        }
+#pragma unroll
+        for (int it = 0; it < XIT; ++it) {
+            const int cm = warp + it * (TC_THREADS / 32);
+            const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
+            const int b = b0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
+            yv[it] = b < nimg ? Y[b * img_stride + yrow + i0 + (k >> 1)] : make_float2(0.f, 0.f);
+        }
+#pragma unroll
+        for (int it = 0; it < AIT; ++it) {
+            const int cm = warp + it * (TC_THREADS / 32);
+            const int rg = cm / (TC_KC / 4);
+            const int m = m0 + rg * 8 + (lane >> 2), k = (cm % (TC_KC / 4)) * 4 + (lane & 3);
+            const int outhalf = m >= N ? 1 : 0;
             const int c = k & 1;
+            const float2 w = wv[it];
             const float v = outhalf == 0 ? (c == 0 ? w.x : -w.y) : (c == 0 ? w.y : w.x);
             const uint32_t hi = to_tf32(v);
             const uint32_t lo = to_tf32(v - __uint_as_float(hi));
@@ -203,14 +225,11 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
             *reinterpret_cast<uint32_t*>(a_hi + off) = hi;
             *reinterpret_cast<uint32_t*>(a_lo + off) = lo;
         }
-        for (int cm = warp; cm < (BP / 8) * (TC_KC / 4); cm += TC_THREADS / 32) {
-            const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
-            const int b = b0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
-            float v = 0.f;
-            if (b < nimg) {
-                const float2 y = Y[b * img_stride + yrow + i0 + (k >> 1)];
-                v = (k & 1) ? y.y : y.x;
-            }
+#pragma unroll
+        for (int it = 0; it < XIT; ++it) {
+            const int cm = warp + it * (TC_THREADS / 32);
+            const int k = (cm % (TC_KC / 4)) * 4 + (lane & 3);
+            const float v = (k & 1) ? yv[it].y : yv[it].x;
             const uint32_t hi = to_tf32(v);
             const uint32_t lo = to_tf32(v - __uint_as_float(hi));
             const int off = cm * 128 + lane * 4;

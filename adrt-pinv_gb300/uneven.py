@@ -13,12 +13,13 @@ import torch
 
 class UnevenBatch:
     def __init__(self, groups, device="cuda"):
-        """groups: [(inverse, count)], one entry per class (distinct inverses)."""
+        """groups: [(inverse, count)], one entry per class; an inverse may appear more than once (a large class split
+        into several concurrent parts), each entry getting its own pipeline."""
+        from .device import Pipeline
+
         self.groups = [(inv, int(c)) for inv, c in groups if int(c) > 0]
-        if len({id(inv) for inv, _ in self.groups}) != len(self.groups):
-            raise ValueError("each class needs its own inverse")
         self.device = torch.device(device)
-        self.pipes = [inv.pipeline(c) for inv, c in self.groups]
+        self.pipes = [Pipeline(inv.plan, c, inv.precision, self.device, inv.stencil_precision) for inv, c in self.groups]
         self.inputs = [torch.zeros((c, 4, 2 * inv.N - 1, inv.N), dtype=torch.float64, device=self.device)
                        for inv, c in self.groups]
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.groups]
