@@ -176,25 +176,14 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
         }
     };
 
-    for (int kc = 0; kc < kchunks; ++kc) {
-        const int s = kc & 1;
-        unsigned char* a_hi = smem_raw + s * STAGE;
-        unsigned char* a_lo = a_hi + A_BYTES;
-        unsigned char* x_hi = a_lo + A_BYTES;
-        unsigned char* x_lo = x_hi + X_BYTES;
-        if (kc >= 2) {
-            // chunk kc-2 used this stage and accumulator: wait for its MMAs, fold its partial in
-            const int waited = mbar_wait(smem_addr(&mbar[s]), (uint32_t)(((kc - 2) >> 1) & 1)) ? 1 : 0;
-            ok = __syncthreads_and(waited) != 0;
-            if (!ok) break;
-            promote(s);
-        }
+    // operand tiles: every thread issues all its loads of a chunk at once (AIT + XIT independent loads in flight),
+    // one chunk ahead: the loads of chunk kc + 1 are issued right after the MMAs of chunk kc and land while the
+    // MMAs of chunk kc - 1 are awaited and folded in; core matrix cm = warp + it * 8
+    constexpr int AIT = (TC_M / 8) * (TC_KC / 4) / (TC_THREADS / 32);
+    constexpr int XIT = (BP / 8) * (TC_KC / 4) / (TC_THREADS / 32);
+    float2 wv[AIT], yv[XIT];
+    auto load_chunk = [&](int kc) {
         const int i0 = kc * (TC_KC / 2);
-        // operand tiles: every thread issues all its loads of the chunk first (AIT + XIT independent loads in
-        // flight), then splits and stores them; core matrix cm = warp + it * 8
-        constexpr int AIT = (TC_M / 8) * (TC_KC / 4) / (TC_THREADS / 32);
-        constexpr int XIT = (BP / 8) * (TC_KC / 4) / (TC_THREADS / 32);
-        float2 wv[AIT], yv[XIT];
 #pragma unroll
         for (int it = 0; it < AIT; ++it) {
             const int cm = warp + it * (TC_THREADS / 32);
@@ -209,6 +198,22 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
             const int rg = cm / (TC_KC / 4), kg = cm % (TC_KC / 4);
             const int b = b0 + rg * 8 + (lane >> 2), k = kg * 4 + (lane & 3);
             yv[it] = b < nimg ? Y[b * img_stride + yrow + i0 + (k >> 1)] : make_float2(0.f, 0.f);
+        }
+    };
+    load_chunk(0);
+
+    for (int kc = 0; kc < kchunks; ++kc) {
+        const int s = kc & 1;
+        unsigned char* a_hi = smem_raw + s * STAGE;
+        unsigned char* a_lo = a_hi + A_BYTES;
+        unsigned char* x_hi = a_lo + A_BYTES;
+        unsigned char* x_lo = x_hi + X_BYTES;
+        if (kc >= 2) {
+            // chunk kc-2 used this stage and accumulator: wait for its MMAs, fold its partial in
+            const int waited = mbar_wait(smem_addr(&mbar[s]), (uint32_t)(((kc - 2) >> 1) & 1)) ? 1 : 0;
+            ok = __syncthreads_and(waited) != 0;
+            if (!ok) break;
+            promote(s);
         }
 #pragma unroll
         for (int it = 0; it < AIT; ++it) {
@@ -257,6 +262,7 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
                              smem_addr(&mbar[s]))
                          : "memory");
         }
+        if (kc + 1 < kchunks) load_chunk(kc + 1);
     }
     // drain: the last two chunks
     if (ok) {
