@@ -161,6 +161,7 @@ def traffic_per_launch():
 def run_reference(args):
     """CPU reference arm: the reference's C++ row kernels + NumPy glue on the host cores, same workload."""
     rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
     if rank != 0:
         return
     import __graft_entry__ as ge
@@ -192,7 +193,7 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "recon/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config(args, 1) | {"global_batch": 1},
+            "config": config(args, world),
             "cpu_baseline": {"value": v, "unit": "recon/s", "cores": threads, "kind": H.eng.kind,
                              "sample": f"one N={N} sinogram per step (the batch's first), same plan"},
             "e2e": {"value": v, "unit": "recon/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
