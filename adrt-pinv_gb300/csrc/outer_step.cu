@@ -83,32 +83,40 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
             const ptrdiff_t off = cur - bufA;  // the current iterate lives at the same offset in every CTA
             const T* upc = up ? up + off : nullptr;
             const T* dnc = dn ? dn + off : nullptr;
+            // the step reads cur (and s) and writes only prv: distinct buffers, so loads of later row pairs may be
+            // issued ahead of earlier stores
+            const T* __restrict__ cr = cur;
+            T* __restrict__ pv = prv;
+            const T* __restrict__ sr = s;
             for (int j = j0; j < N; j += CPP) {
                 const int jp = j ^ 1;
                 const bool hl = j > 0, hr = j < N - 1;
-#pragma unroll 4
-                for (int m = grp; m < BAND / 2; m += RG) {
+                constexpr int ITS = (BAND / 2 + RG - 1) / RG;  // row pairs per thread (compile-time trip count)
+#pragma unroll
+                for (int it = 0; it < ITS; ++it) {
+                    const int m = grp + it * RG;
+                    if (ITS * RG > BAND / 2 && m >= BAND / 2) break;
                     const int r0 = 2 * m, r1 = r0 + 1;
-                    const T c0 = cur[r0 * N + j], c1 = cur[r1 * N + j];
-                    const T q0 = cur[r0 * N + jp], q1 = cur[r1 * N + jp];
-                    const T qm = r0 > 0 ? cur[(r0 - 1) * N + jp] : (upc ? upc[(BAND - 1) * N + jp] : (T)0);
-                    const T qp = r1 < BAND - 1 ? cur[(r1 + 1) * N + jp] : (dnc ? dnc[jp] : (T)0);
+                    const T c0 = cr[r0 * N + j], c1 = cr[r1 * N + j];
+                    const T q0 = cr[r0 * N + jp], q1 = cr[r1 * N + jp];
+                    const T qm = r0 > 0 ? cr[(r0 - 1) * N + jp] : (upc ? upc[(BAND - 1) * N + jp] : (T)0);
+                    const T qp = r1 < BAND - 1 ? cr[(r1 + 1) * N + jp] : (dnc ? dnc[jp] : (T)0);
                     T b0 = (T)2 * c1, b1 = (T)2 * c0;
                     if (hl) {
-                        b0 += cur[r1 * N + j - 1];
-                        b1 += cur[r0 * N + j - 1];
+                        b0 += cr[r1 * N + j - 1];
+                        b1 += cr[r0 * N + j - 1];
                     }
                     if (hr) {
-                        b0 += cur[r1 * N + j + 1];
-                        b1 += cur[r0 * N + j + 1];
+                        b0 += cr[r1 * N + j + 1];
+                        b1 += cr[r0 * N + j + 1];
                     }
                     const T a0 = ((T)2 * q0 + qm) + q1;  // K along rows (i-1 term first, then i+1)
                     const T a1 = ((T)2 * q1 + q0) + qp;
                     const T g0 = ((T)8 * c0 + a0) + b0;
                     const T g1 = ((T)8 * c1 + a1) + b1;
                     const int e0 = r0 * N + j, e1 = r1 * N + j;
-                    prv[e0] = c0 + om_a * (s[e0] - g0) + om_1 * (c0 - prv[e0]);
-                    prv[e1] = c1 + om_a * (s[e1] - g1) + om_1 * (c1 - prv[e1]);
+                    pv[e0] = c0 + om_a * (sr[e0] - g0) + om_1 * (c0 - pv[e0]);
+                    pv[e1] = c1 + om_a * (sr[e1] - g1) + om_1 * (c1 - pv[e1]);
                 }
             }
             cluster.sync();
