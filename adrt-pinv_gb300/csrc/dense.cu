@@ -65,6 +65,61 @@ __global__ void __launch_bounds__(256) dense_simt_kernel(int N, int nimg, const 
     }
 }
 
+// Small batches (nimg <= 8, FP32): the product streams each operator once from HBM, so the kernel is built for that
+// stream. The operator comes transposed, WT_r[i][o] = W_r[o][i], each thread owns one output row o and walks i, so
+// a warp reads 32 consecutive complex values per i (coalesced), with eight loads in flight per thread; the images'
+// input rows are staged in shared memory in chunks of DS_IC and read as broadcasts. FP32 FMA accumulation in two levels.
+constexpr int DS_THREADS = 256;
+constexpr int DS_IC = 512;
+constexpr int DS_SUB = 128;
+template <int NB>
+__global__ void __launch_bounds__(DS_THREADS) dense_stream_kernel(int N, int nimg, const int* __restrict__ rows,
+                                                                  const float2* __restrict__ WT,
+                                                                  const float2* __restrict__ Y, long long img_stride,
+                                                                  float2* __restrict__ Zd) {
+    __shared__ float2 ys[NB][DS_IC];
+    const int r = blockIdx.x;
+    const int o = blockIdx.y * DS_THREADS + threadIdx.x;
+    const long long yrow = (long long)rows[r] * N;
+    const bool live = o < N;
+    float2 acc[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b) acc[b] = make_float2(0.f, 0.f);
+    for (int i0 = 0; i0 < N; i0 += DS_IC) {
+        const int ic = N - i0 < DS_IC ? N - i0 : DS_IC;
+        __syncthreads();
+        for (int e = threadIdx.x; e < NB * ic; e += DS_THREADS) {
+            const int b = e / ic, i = e - (e / ic) * ic;
+            ys[b][i] = b < nimg ? Y[b * img_stride + yrow + i0 + i] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        if (live) {
+            const float2* w = WT + ((size_t)r * N + i0) * N + o;
+            // two-level sum: a fresh partial every DS_SUB terms, added into the total (round-off grows with
+            // sqrt(DS_SUB) + sqrt(N / DS_SUB) instead of sqrt(N))
+            for (int ib = 0; ib < ic; ib += DS_SUB) {
+                const int ie = ic - ib < DS_SUB ? ic : ib + DS_SUB;
+                float2 part[NB];
+#pragma unroll
+                for (int b = 0; b < NB; ++b) part[b] = make_float2(0.f, 0.f);
+#pragma unroll 8
+                for (int i = ib; i < ie; ++i) {
+                    const float2 wv = w[(size_t)i * N];
+#pragma unroll
+                    for (int b = 0; b < NB; ++b) part[b] = cfma(wv, ys[b][i], part[b]);
+                }
+#pragma unroll
+                for (int b = 0; b < NB; ++b) acc[b] = cadd(acc[b], part[b]);
+            }
+        }
+    }
+    if (live) {
+#pragma unroll
+        for (int b = 0; b < NB; ++b)
+            if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = acc[b];
+    }
+}
+
 // ------------------------------------------------------------------ tcgen05 (sm_100 family) helpers
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -314,7 +369,21 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
     if (!nimg || !nrows) return ADRT_OK;
     const int N = 1 << n;
     int rc;
-    if (dtype == ADRT_F32 && use_tc && n >= 6) {
+    if (use_tc == 2) {
+        if (dtype != ADRT_F32 || nimg > 8) {
+            set_error("dense_rows: the streaming kernel (use_tc = 2) takes FP32 and at most 8 images (nimg=%d)", nimg);
+            return ADRT_EINVAL;
+        }
+        dim3 grid(nrows, (N + DS_THREADS - 1) / DS_THREADS);
+        const float2* Wt = reinterpret_cast<const float2*>(W);
+        const float2* Yf = reinterpret_cast<const float2*>(Y);
+        float2* Zf = reinterpret_cast<float2*>(Zd);
+        if (nimg <= 1) dense_stream_kernel<1><<<grid, DS_THREADS, 0, st>>>(N, nimg, rows, Wt, Yf, img_stride, Zf);
+        else if (nimg <= 2) dense_stream_kernel<2><<<grid, DS_THREADS, 0, st>>>(N, nimg, rows, Wt, Yf, img_stride, Zf);
+        else if (nimg <= 4) dense_stream_kernel<4><<<grid, DS_THREADS, 0, st>>>(N, nimg, rows, Wt, Yf, img_stride, Zf);
+        else dense_stream_kernel<8><<<grid, DS_THREADS, 0, st>>>(N, nimg, rows, Wt, Yf, img_stride, Zf);
+        rc = launch_status("dense_stream_kernel");
+    } else if (dtype == ADRT_F32 && use_tc && n >= 6) {
         if (!err) { set_error("dense_rows: the tensor-core path needs an error flag"); return ADRT_EINVAL; }
         if (nimg <= 16) rc = launch_tc<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
         else if (nimg <= 32) rc = launch_tc<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);

@@ -56,6 +56,9 @@ class RowTables:
         self.count = 0  # level-rows applied, counted as the reference does
         self.timer = None  # list: when set, (start, end) CUDA events of every polynomial-row launch are appended
         self.use_tc = real == torch.float32  # dense rows on tensor cores in FP32
+        # small batches (<= 8 images, FP32): the streaming CUDA-core kernel, with the operators stored transposed;
+        # set by the owning pipeline before the first dense table is built
+        self.stream_dense = False
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self._zd = None
 
@@ -117,11 +120,14 @@ class RowTables:
                 sel = torch.from_numpy(self.dense_sel).to(self.device)
                 for c0, T in dense_row_operator_device(self.plan, fold_pre, fold_post, pre_b1, post_b1t, self.device):
                     hit = ((sel >= c0) & (sel < c0 + T.shape[0])).nonzero().flatten()
-                    out[hit] = T[sel[hit] - c0].to(out.dtype)
+                    Th = T[sel[hit] - c0]
+                    out[hit] = (Th.transpose(-1, -2) if self.stream_dense else Th).to(out.dtype)
                 self._dense_dev[key] = out
             else:
-                T = self.plan.dense_row_operator(fold_pre, fold_post, pre_b1, post_b1t)
-                self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T[self.dense_sel])).to(
+                T = self.plan.dense_row_operator(fold_pre, fold_post, pre_b1, post_b1t)[self.dense_sel]
+                if self.stream_dense:
+                    T = T.transpose(0, 2, 1)
+                self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T)).to(
                     device=self.device, dtype=_cdtype(self.real))
         return self._dense_dev[key]
 
@@ -134,13 +140,15 @@ class RowTables:
                                "were not written")
 
     def dense_apply(self, Y, T):
-        """Y[b, r] <- T_r Y[b, r] for the dense rows (tensor cores in FP32, CUDA cores in FP64)."""
+        """Y[b, r] <- T_r Y[b, r] for the dense rows (FP32: tensor cores, or the streaming CUDA-core kernel for small
+        batches; FP64: CUDA cores)."""
         B, R, N = Y.shape
         nd = int(self.rows_dense.numel())
         if self._zd is None or self._zd.shape[1] != B:
             self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
+        mode = 2 if self.stream_dense else (1 if self.use_tc else 0)
         C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(T), C.ptr(Y), R * N,
-               C.ptr(self._zd), C.ptr(self.err), 1 if self.use_tc else 0, C.stream_handle())
+               C.ptr(self._zd), C.ptr(self.err), mode, C.stream_handle())
 
     def run(self, Y, ops):
         """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take the exact
@@ -204,6 +212,16 @@ def _rows_apply_f64(X, z_rows, ops, n, counter):
     C.call("adrt_rows_run", ctypes.byref(j), st)
 
 
+def _load_torch_linalg():
+    """torch opens its CUDA linear-algebra library lazily by file name; where a profiler's library injection changes
+    the search path that lookup fails, so the library is loaded once by its full path first."""
+    import os
+
+    p = os.path.join(os.path.dirname(torch.__file__), "lib", "libtorch_cuda_linalg.so")
+    if os.path.exists(p):
+        ctypes.CDLL(p, mode=ctypes.RTLD_GLOBAL)
+
+
 def dense_row_operator_device(plan: Plan, fold_pre, fold_post, pre_b1, post_b1t, device, chunk=None):
     """Plan.dense_row_operator built on the device in FP64, in chunks of dense frequencies: yields (first index,
     (k, N, N) complex128). The Gram matrices M_k and every butterfly fold come from the library's own FP64 row
@@ -217,6 +235,8 @@ def dense_row_operator_device(plan: Plan, fold_pre, fold_post, pre_b1, post_b1t,
     n, N, Kd, tau = plan.n, plan.N, len(plan.dense_freqs), plan.tau
     lo, hi = plan.p_levels
     dev = torch.device(device)
+    if dev.type == "cuda":
+        _load_torch_linalg()
     z = torch.from_numpy(roots_of_unity(plan.L)[plan.dense_freqs]).to(dev)
     if chunk is None:
         chunk = max(1, min(Kd, (1 << 29) // (N * N * 16)))  # about 512 MB per (k, N, N) block
@@ -273,6 +293,7 @@ class Pipeline:
         self.outer_real = torch.float64
         self.stencil_real = PRECISIONS[stencil_precision or precision]
         self.tables = RowTables(plan, self.real, self.device)
+        self.tables.stream_dense = self.real == torch.float32 and self.B <= 8
         N, L, B = plan.N, plan.L, self.B
         dev = self.device
         self.Y = torch.empty((B, 2 * L, N), dtype=_cdtype(self.real), device=dev)

@@ -551,6 +551,12 @@ def run_large(args):
             torch.cuda.synchronize()
             ms_b = e0.elapsed_time(e1) / steps
             res[f"batch{B}"] = {"ms_per_apply": ms_b, "recon_s": B / (ms_b * 1e-3)}
+    if args.profile_region:  # one more batch-8 replay as the profiled region (per-kernel launch lists)
+        torch.cuda.synchronize()
+        torch.cuda.profiler.start()
+        pipe.replay(b[:8].contiguous())
+        torch.cuda.synchronize()
+        torch.cuda.profiler.stop()
     got = pipe.x_out[0].cpu().numpy()
     ref = H.pipeline(1, "fp64").apply(b[:1].contiguous())[0].cpu().numpy()
     line = {"metric": "hybrid-inverse recon/s at N=2048 (batch 8)", "value": res["batch8"]["recon_s"],

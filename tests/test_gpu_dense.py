@@ -46,6 +46,39 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
     assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
 
 
+@pytest.mark.parametrize("n,nimg,nrows", [(6, 1, 3), (8, 3, 5), (9, 8, 2), (11, 2, 1)])
+def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
+    """The small-batch streaming kernel (use_tc = 2, operators transposed) against the FP64 product; it refuses more
+    than 8 images."""
+    import torch
+
+    C = pkg._lib
+    C.load()
+    N, R = 1 << n, 8
+    rng = np.random.default_rng(n + nimg)
+    W = (rng.standard_normal((nrows, N, N)) + 1j * rng.standard_normal((nrows, N, N))) / np.sqrt(N)
+    Y = rng.standard_normal((nimg, R, N)) + 1j * rng.standard_normal((nimg, R, N))
+    rows = np.array(sorted(rng.choice(R, nrows, replace=False)), dtype=np.int32)
+    ref = Y.copy()
+    for i, r in enumerate(rows):
+        ref[:, r, :] = Y[:, r, :] @ W[i].T
+    WT = torch.from_numpy(np.ascontiguousarray(W.transpose(0, 2, 1))).to("cuda", torch.complex64)
+    Yd = torch.from_numpy(Y).to("cuda", torch.complex64)
+    rd = torch.from_numpy(rows).cuda()
+    Zd = torch.empty((nrows, nimg, N), dtype=torch.complex64, device="cuda")
+    C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Yd), R * N, C.ptr(Zd), None, 2,
+           C.stream_handle())
+    out = Yd.cpu().numpy()
+    for r in range(R):
+        e = np.linalg.norm(out[:, r, :] - ref[:, r, :]) / np.linalg.norm(ref[:, r, :])
+        assert e < 1e-6, (r, e)
+    Z9 = torch.empty((nrows, 9, N), dtype=torch.complex64, device="cuda")
+    Y9 = torch.zeros((9, R, N), dtype=torch.complex64, device="cuda")
+    rc = C.load().adrt_dense_rows(C.F32, n, 9, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Y9), R * N, C.ptr(Z9), None, 2,
+                                  C.stream_handle())
+    assert rc != 0
+
+
 @pytest.mark.parametrize("method", ["hybrid", "lp"])
 def test_device_built_dense_operators_match_host(pkg, method):
     """Dense-row operators built on the device (FP64 row kernels on unit vectors + Cholesky, used for n >= 9) equal
