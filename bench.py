@@ -499,8 +499,8 @@ def run_uneven(args):
     # the same classes one after another, eager (no graph, no concurrency)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
-    for inv, x in zip([g[0] for g in groups], sinos):
-        inv.pipeline(x.shape[0]).apply(x)
+    for pipe, x in zip(U.pipes, sinos):
+        pipe.apply(x)
     torch.cuda.synchronize()
     eager_ms = (time.perf_counter() - t1) * 1e3
     outs = [o.clone() for o in U.replay()]
