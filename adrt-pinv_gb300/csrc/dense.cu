@@ -65,8 +65,8 @@ __global__ void __launch_bounds__(256) dense_simt_kernel(int N, int nimg, const 
     }
 }
 
-// Small batches (nimg <= 8, FP32): the product streams each operator once from HBM, so the kernel is built for that
-// stream. The operator comes transposed, WT_r[i][o] = W_r[o][i], each thread owns one output row o and walks i, so
+// Small batches (nimg <= 16, FP32): the product streams each operator from HBM once per group of up to 8 images, so
+// the kernel is built for that stream. The operator comes transposed, WT_r[i][o] = W_r[o][i], each thread owns one output row o and walks i, so
 // a warp reads 32 consecutive complex values per i (coalesced), with eight loads in flight per thread; the images'
 // input rows are staged in shared memory in chunks of DS_IC and read as broadcasts. FP32 FMA accumulation in two levels.
 constexpr int DS_THREADS = 256;
@@ -80,6 +80,7 @@ __global__ void __launch_bounds__(DS_THREADS) dense_stream_kernel(int N, int nim
     __shared__ float2 ys[NB][DS_IC];
     const int r = blockIdx.x;
     const int o = blockIdx.y * DS_THREADS + threadIdx.x;
+    const int b0 = blockIdx.z * NB;  // images b0 .. b0 + NB - 1 (one pass over the operators per group of NB)
     const long long yrow = (long long)rows[r] * N;
     const bool live = o < N;
     float2 acc[NB];
@@ -90,7 +91,7 @@ __global__ void __launch_bounds__(DS_THREADS) dense_stream_kernel(int N, int nim
         __syncthreads();
         for (int e = threadIdx.x; e < NB * ic; e += DS_THREADS) {
             const int b = e / ic, i = e - (e / ic) * ic;
-            ys[b][i] = b < nimg ? Y[b * img_stride + yrow + i0 + i] : make_float2(0.f, 0.f);
+            ys[b][i] = b0 + b < nimg ? Y[(b0 + b) * img_stride + yrow + i0 + i] : make_float2(0.f, 0.f);
         }
         __syncthreads();
         if (live) {
@@ -116,7 +117,7 @@ __global__ void __launch_bounds__(DS_THREADS) dense_stream_kernel(int N, int nim
     if (live) {
 #pragma unroll
         for (int b = 0; b < NB; ++b)
-            if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = acc[b];
+            if (b0 + b < nimg) Zd[((size_t)r * nimg + b0 + b) * N + o] = acc[b];
     }
 }
 
@@ -370,11 +371,11 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
     const int N = 1 << n;
     int rc;
     if (use_tc == 2) {
-        if (dtype != ADRT_F32 || nimg > 8) {
-            set_error("dense_rows: the streaming kernel (use_tc = 2) takes FP32 and at most 8 images (nimg=%d)", nimg);
+        if (dtype != ADRT_F32 || nimg > 16) {
+            set_error("dense_rows: the streaming kernel (use_tc = 2) takes FP32 and at most 16 images (nimg=%d)", nimg);
             return ADRT_EINVAL;
         }
-        dim3 grid(nrows, (N + DS_THREADS - 1) / DS_THREADS);
+        dim3 grid(nrows, (N + DS_THREADS - 1) / DS_THREADS, nimg > 8 ? (nimg + 7) / 8 : 1);
         const float2* Wt = reinterpret_cast<const float2*>(W);
         const float2* Yf = reinterpret_cast<const float2*>(Y);
         float2* Zf = reinterpret_cast<float2*>(Zd);

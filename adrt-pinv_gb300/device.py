@@ -56,7 +56,7 @@ class RowTables:
         self.count = 0  # level-rows applied, counted as the reference does
         self.timer = None  # list: when set, (start, end) CUDA events of every polynomial-row launch are appended
         self.use_tc = real == torch.float32  # dense rows on tensor cores in FP32
-        # small batches (<= 8 images, FP32): the streaming CUDA-core kernel, with the operators stored transposed;
+        # small batches (<= 16 images, FP32): the streaming CUDA-core kernel, with the operators stored transposed;
         # set by the owning pipeline before the first dense table is built
         self.stream_dense = False
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
@@ -293,7 +293,7 @@ class Pipeline:
         self.outer_real = torch.float64
         self.stencil_real = PRECISIONS[stencil_precision or precision]
         self.tables = RowTables(plan, self.real, self.device)
-        self.tables.stream_dense = self.real == torch.float32 and self.B <= 8
+        self.tables.stream_dense = self.real == torch.float32 and self.B <= 16
         N, L, B = plan.N, plan.L, self.B
         dev = self.device
         self.Y = torch.empty((B, 2 * L, N), dtype=_cdtype(self.real), device=dev)

@@ -165,9 +165,9 @@ int adrt_outer_step_max_n(int dtype);
  *   Y[b, rows[r], :] <- W_r Y[b, rows[r], :]     (W: nrows x N x N complex, row-major, dtype; Y rows of N complex at
  *   image stride img_stride complex elements), computed out of place in Zd (nrows x nimg x N complex scratch) and
  * copied back. use_tc = 1 with FP32 and n >= 6: tensor cores (tcgen05.mma kind::tf32, 3xTF32 split, FP32 accumulate);
- * *err (device int) is set to 1 if a tensor-core completion wait ran out. use_tc = 2 (FP32, nimg <= 8): W is given
- * TRANSPOSED (W[r][i][o] = W_r[o][i]) and a CUDA-core kernel streams it once (small batches, where the product is
- * bound by reading the operators). Otherwise (use_tc = 0) CUDA cores. */
+ * *err (device int) is set to 1 if a tensor-core completion wait ran out. use_tc = 2 (FP32, nimg <= 16): W is given
+ * TRANSPOSED (W[r][i][o] = W_r[o][i]) and a CUDA-core kernel streams it once per group of 8 images (small batches,
+ * where the product is bound by reading the operators). Otherwise (use_tc = 0) CUDA cores. */
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
                     long long img_stride, void* Zd, int32_t* err, int use_tc, void* stream);
 

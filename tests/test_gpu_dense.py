@@ -46,10 +46,10 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
     assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
 
 
-@pytest.mark.parametrize("n,nimg,nrows", [(6, 1, 3), (8, 3, 5), (9, 8, 2), (11, 2, 1)])
+@pytest.mark.parametrize("n,nimg,nrows", [(6, 1, 3), (8, 3, 5), (9, 8, 2), (11, 2, 1), (7, 13, 3), (10, 16, 1)])
 def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
-    """The small-batch streaming kernel (use_tc = 2, operators transposed) against the FP64 product; it refuses more
-    than 8 images."""
+    """The small-batch streaming kernel (use_tc = 2, operators transposed, passes of 8 images) against the FP64
+    product; it refuses more than 16 images."""
     import torch
 
     C = pkg._lib
@@ -72,9 +72,9 @@ def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
     for r in range(R):
         e = np.linalg.norm(out[:, r, :] - ref[:, r, :]) / np.linalg.norm(ref[:, r, :])
         assert e < 1e-6, (r, e)
-    Z9 = torch.empty((nrows, 9, N), dtype=torch.complex64, device="cuda")
-    Y9 = torch.zeros((9, R, N), dtype=torch.complex64, device="cuda")
-    rc = C.load().adrt_dense_rows(C.F32, n, 9, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Y9), R * N, C.ptr(Z9), None, 2,
+    Z9 = torch.empty((nrows, 17, N), dtype=torch.complex64, device="cuda")
+    Y9 = torch.zeros((17, R, N), dtype=torch.complex64, device="cuda")
+    rc = C.load().adrt_dense_rows(C.F32, n, 17, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Y9), R * N, C.ptr(Z9), None, 2,
                                   C.stream_handle())
     assert rc != 0
 
