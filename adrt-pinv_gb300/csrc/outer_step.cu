@@ -152,10 +152,9 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     }
 }
 
-template <typename T, int n>
-static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
+template <typename T, int n, int BAND>
+static int launch_os_band(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     constexpr int N = 1 << n;
-    constexpr int BAND = N >= 32 ? 32 : N;
     constexpr int CL = N / BAND;
     const size_t smem = 3 * (size_t)BAND * N * sizeof(T);
     auto kern = outer_step_kernel<T, n, BAND>;
@@ -179,6 +178,17 @@ static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     cfg.numAttrs = 1;
     cudaLaunchKernelEx(&cfg, kern, A);
     return launch_status("outer_step_kernel");
+}
+
+// 32-row bands; when the batch's clusters cannot fill the SMs (N <= 256), 16-row bands instead: twice the CTAs per
+// image (clusters of up to 16), half the rows each, so a small batch finishes its stencil steps sooner
+template <typename T, int n>
+static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
+    constexpr int N = 1 << n;
+    if constexpr (N >= 32 && N / 16 <= 16) {
+        if ((long)nimg * (N / 32) < device_sm_count()) return launch_os_band<T, n, 16>(A, nimg, st);
+    }
+    return launch_os_band<T, n, (N >= 32 ? 32 : N)>(A, nimg, st);
 }
 
 // largest n with a fused (cluster) outer step for element type T: the band tiles must fit 227 KB and the cluster

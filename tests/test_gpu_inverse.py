@@ -158,9 +158,11 @@ def test_batch_equals_single(pkg, hybrid256):
 
 
 @pytest.mark.parametrize("prec", ["fp32", "fp64"])
-@pytest.mark.parametrize("n,precond", [(5, "g1"), (8, "g1"), (8, "lorr"), (9, "g1"), (6, "none")])
-def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond):
-    """adrt_outer_step (residual + P + outer update, one clustered kernel) equals resid / g1 steps / outer kernels."""
+@pytest.mark.parametrize("n,precond,nimg", [(5, "g1", 3), (8, "g1", 3), (8, "g1", 40), (8, "lorr", 3), (9, "g1", 3),
+                                             (6, "none", 3)])
+def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond, nimg):
+    """adrt_outer_step (residual + P + outer update, one clustered kernel) equals resid / g1 steps / outer kernels;
+    3 images take 16-row bands (N <= 256), 40 images at N=256 the 32-row bands."""
     import torch
 
     if prec == "fp64" and n > 8:
@@ -168,13 +170,13 @@ def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond):
     N = 1 << n
     method = "lp" if precond == "none" else "hybrid"
     plan = pkg.Plan(method, n, np.full(2 * N, 4.0), precond="g1" if precond == "none" else precond, outer=(1.0, 2.0, 3))
-    pipe = pkg.Pipeline(plan, 3, prec)
+    pipe = pkg.Pipeline(plan, nimg, prec)
     assert pipe.fused_outer_ok()
     g = torch.Generator(device="cuda").manual_seed(n)
-    y = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
+    y = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
     pipe.parts.normal_(generator=g)
-    x = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
-    xp = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=g)
+    x = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    xp = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
     out_f = torch.empty_like(x)
     out_s = torch.empty_like(x)
     pipe.fused_outer_step(y, True, x, xp, out_f, 0.7, 0.3, 0.0)
