@@ -436,16 +436,20 @@ class Pipeline:
             self.apply(self.b_in)
             side.synchronize()
             self.graph = torch.cuda.CUDAGraph()
+            before = self.tables.count
             with torch.cuda.graph(self.graph, stream=side):
                 self.x_out = self.apply(self.b_in)
+            self.graph_count = self.tables.count - before  # level-rows of one replay
         torch.cuda.current_stream(self.device).wait_stream(side)
         return self
 
     def replay(self, b=None):
-        """Run the captured apply on the current stream (b copied into the graph's input buffer first)."""
+        """Run the captured apply on the current stream (b copied into the graph's input buffer first; a host tensor
+        is copied straight from host memory)."""
         if b is not None:
             self.b_in.copy_(b, non_blocking=True)
         self.graph.replay()
+        self.tables.count += self.graph_count
         return self.x_out
 
     def apply(self, b):

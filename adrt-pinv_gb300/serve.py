@@ -39,8 +39,8 @@ class Lane:
         self.inv, self.slots = inverse, int(slots)
         self.N = inverse.N
         self.stream = torch.cuda.Stream(device=device)
-        with torch.cuda.stream(self.stream):
-            self.pipe = inverse.pipeline(self.slots).capture()
+        with torch.cuda.stream(self.stream):  # the lane's own pipeline: nothing shared with inverse.apply()
+            self.pipe = Pipeline(inverse.plan, self.slots, inverse.precision, device, inverse.stencil_precision).capture()
         self.stream.synchronize()
         self.stage_in = torch.zeros((self.slots, 4, 2 * self.N - 1, self.N), dtype=torch.float64, pin_memory=True)
         self.stage_out = torch.empty((self.slots, self.N, self.N), dtype=torch.float64, pin_memory=True)
@@ -86,7 +86,6 @@ class Lane:
 
     def release(self):
         """Drop the captured graph and the pipeline's buffers."""
-        self.inv._pipes.pop((self.slots, self.inv.precision), None)
         self.pipe = None
 
 

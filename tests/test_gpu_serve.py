@@ -76,3 +76,18 @@ def test_served_mix_under_small_budget(pkg, golden):
     big = max(serve.Lane.estimate_bytes(invs[n], 4) for n in invs)
     S, _ = _serve(pkg, golden, big + 1, 1)
     assert S.evictions >= 1 and S.memory_in_use() <= big + 1
+
+
+def test_public_apply_graph_replay(pkg, golden):
+    """apply() runs eagerly on the first call of a batch size and replays a CUDA graph from the second: the results
+    and the level-row count per call stay the same."""
+    inv = _inverses(pkg, golden)[6]
+    bs = np.stack(_sinos(pkg, 6, 2, 40))
+    outs, counts = [], []
+    for _ in range(3):
+        c0 = inv.eng.count[0]
+        outs.append(inv.apply(bs))
+        counts.append(inv.eng.count[0] - c0)
+    assert inv.pipeline(2).graph is not None
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+    assert counts[0] == counts[1] == counts[2] > 0
