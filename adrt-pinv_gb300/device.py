@@ -59,6 +59,7 @@ class RowTables:
         # small batches (<= 16 images, FP32): the streaming CUDA-core kernel, with the operators stored transposed;
         # set by the owning pipeline before the first dense table is built
         self.stream_dense = False
+        self.row_grid = 0  # CTAs of the row programs (0: one per SM); set by the autotuner
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self._zd = None
 
@@ -83,7 +84,7 @@ class RowTables:
         for i, (op, lo, hi) in enumerate(ops):
             j.op[i], j.lo[i], j.hi[i] = OPCODE[op], lo, hi
         j.counter = self.counter.data_ptr()
-        j.grid = 0
+        j.grid = self.row_grid
         return j
 
     def _timed_main(self, Y, ops, st):
@@ -112,7 +113,7 @@ class RowTables:
     def dense_table(self, fold_pre, fold_post, pre_b1=False, post_b1t=False):
         """The folded dense-row operators of one op list, one per dense packed row, in the row precision. Built on
         the host in FP64 up to n = 8 and on the device (FP64 torch, Cholesky form) for larger n."""
-        key = (fold_pre, fold_post, pre_b1, post_b1t)
+        key = (fold_pre, fold_post, pre_b1, post_b1t, self.stream_dense)
         if key not in self._dense_dev:
             if self.plan.n >= 9 and self.device.type == "cuda":
                 N = self.plan.N

@@ -1,0 +1,85 @@
+"""Autotuner for the launch configuration of a device pipeline.
+
+Per (plan, batch, precision) the tuner times the candidate configurations of the two choices that depend on the
+workload's shape, on the GPU and with the pipeline's own data, and keeps the fastest:
+  * the dense-row kernel: tensor cores (3xTF32 tcgen05), the streaming CUDA-core kernel (batches of at most 16; the
+    operators stored transposed) or the tiled CUDA-core kernel;
+  * the grid of the row programs: one or two persistent CTAs per SM.
+Each candidate is timed with CUDA events over `reps` applies after one warm-up apply. Results are cached per
+(N, method, degree cap, dense cap, batch, precision, GPU name) in memory and, when a path is given, in a JSON file.
+"""
+
+import itertools
+import json
+import os
+
+import torch
+
+
+def device_info(device):
+    """(name, SM count) of the GPU."""
+    return torch.cuda.get_device_name(device), torch.cuda.get_device_properties(device).multi_processor_count
+
+
+def candidates(pipe):
+    """The configurations worth timing for this pipeline: [{"dense": mode, "row_grid": g}]."""
+    sms = device_info(pipe.device)[1]
+    dense = ["none"]
+    if len(pipe.plan.dense_freqs):
+        if pipe.real == torch.float32:
+            dense = ["tc", "simt"] + (["stream"] if pipe.B <= 16 else [])
+        else:
+            dense = ["simt"]
+    return [{"dense": d, "row_grid": g} for d, g in itertools.product(dense, (sms, 2 * sms))]
+
+
+def apply_config(pipe, cfg):
+    t = pipe.tables
+    t.stream_dense = cfg["dense"] == "stream"
+    t.use_tc = cfg["dense"] == "tc"
+    t.row_grid = int(cfg["row_grid"])
+
+
+def key_of(pipe):
+    p = pipe.plan
+    name = device_info(pipe.device)[0]
+    return f"{name}|N={p.N}|{p.method}|cap={p.deg_cap}|dense={p.dense_cap}|B={pipe.B}|{pipe.precision}"
+
+
+class Tuner:
+    def __init__(self, path=None, reps=3, timer=None):
+        self.path, self.reps = path, int(reps)
+        self.cache = {}
+        if path and os.path.exists(path):
+            with open(path) as f:
+                self.cache = json.load(f)
+        self.timer = timer or self._time
+
+    def _time(self, pipe, b):
+        pipe.apply(b)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(self.reps):
+            pipe.apply(b)
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / self.reps
+
+    def tune(self, pipe, b):
+        """Pick and apply the fastest configuration for pipe on sinograms b (on the device); returns
+        {"config": ..., "ms": {...}}. Must run before the pipeline is captured in a graph."""
+        k = key_of(pipe)
+        if k not in self.cache:
+            times = {}
+            for cfg in candidates(pipe):
+                apply_config(pipe, cfg)
+                times[json.dumps(cfg, sort_keys=True)] = self.timer(pipe, b)
+            best = min(times, key=times.get)
+            self.cache[k] = {"config": json.loads(best), "ms": times}
+            if self.path:
+                with open(self.path, "w") as f:
+                    json.dump(self.cache, f, indent=1)
+        apply_config(pipe, self.cache[k]["config"])
+        t = pipe.tables  # keep only the dense tables of the chosen layout
+        t._dense_dev = {kk: v for kk, v in t._dense_dev.items() if kk[4] == t.stream_dense}
+        return self.cache[k]

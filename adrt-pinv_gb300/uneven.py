@@ -12,9 +12,10 @@ import torch
 
 
 class UnevenBatch:
-    def __init__(self, groups, device="cuda"):
+    def __init__(self, groups, device="cuda", tuner=None, sinos=None):
         """groups: [(inverse, count)], one entry per class; an inverse may appear more than once (a large class split
-        into several concurrent parts), each entry getting its own pipeline."""
+        into several concurrent parts), each entry getting its own pipeline. With a tuner (tune.Tuner) and the
+        classes' sinograms, every class's launch configuration is autotuned on its own data before the capture."""
         from .device import Pipeline
 
         self.groups = [(inv, int(c)) for inv, c in groups if int(c) > 0]
@@ -22,6 +23,10 @@ class UnevenBatch:
         self.pipes = [Pipeline(inv.plan, c, inv.precision, self.device, inv.stencil_precision) for inv, c in self.groups]
         self.inputs = [torch.zeros((c, 4, 2 * inv.N - 1, inv.N), dtype=torch.float64, device=self.device)
                        for inv, c in self.groups]
+        self.tuning = []
+        if tuner is not None and sinos is not None:
+            for pipe, x in zip(self.pipes, sinos):
+                self.tuning.append(tuner.tune(pipe, x.to(self.device)))
         self.streams = [torch.cuda.Stream(device=self.device) for _ in self.groups]
         cap = torch.cuda.Stream(device=self.device)
         cap.wait_stream(torch.cuda.current_stream(self.device))

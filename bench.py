@@ -455,7 +455,7 @@ def run_uneven(args):
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
-    from adrt_pinv_gb300 import inverse, uneven
+    from adrt_pinv_gb300 import inverse, tune, uneven
 
     dev = torch.device("cuda", 0)
     rng = np.random.default_rng(2)
@@ -482,7 +482,13 @@ def run_uneven(args):
                 sinos.append(_phantom_sinos(pkg, n, len(idx), 10000 * n + 100 * p + (m == "lp"), dev, sig[idx]))
                 keys.append((n, m, p))
     setup_s = time.perf_counter() - t0
-    U = uneven.UnevenBatch(groups, device=dev)
+    t1 = time.perf_counter()
+    U = uneven.UnevenBatch(groups, device=dev, tuner=tune.Tuner(), sinos=sinos)
+    tune_s = time.perf_counter() - t1
+    chosen = {}
+    for key, tr in zip(keys, U.tuning):
+        c = tr["config"]
+        chosen[f"N={1 << key[0]} {key[1]} p={key[2]}"] = f"{c['dense']}/grid{c['row_grid']}"
     U.set_inputs(sinos)
     for _ in range(args.warmup):
         U.replay()
@@ -515,6 +521,7 @@ def run_uneven(args):
             "config": {"workload": "512 sinograms, N U{64,128,256,512}, p U{8,16,32,64}, L_p/hybrid 50/50, "
                                    "dense_cap 16 (12 at p=16, none at p=8), FP32 rows + FP64 tables", "classes": len(groups)},
             "eager_sequential_ms": eager_ms, "graph_launches_per_step": 1, "setup_s": setup_s,
+            "autotune_s": tune_s, "autotuned": chosen,
             "device_gb": U.device_bytes() / 1e9, "max_rel_err_vs_fp64": max(errs.values()),
             "rel_err_vs_fp64": errs, "clocks": clk.summary()}
     print(json.dumps(line), flush=True)

@@ -91,3 +91,21 @@ def test_public_apply_graph_replay(pkg, golden):
     assert inv.pipeline(2).graph is not None
     assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
     assert counts[0] == counts[1] == counts[2] > 0
+
+
+def test_autotuned_pipeline_same_results(pkg, golden):
+    """The autotuner times every candidate launch configuration on the GPU and keeps the fastest; the tuned pipeline
+    gives the same inverse (within FP32 rounding of the dense kernels, 1e-6)."""
+    import torch
+
+    from adrt_pinv_gb300 import tune
+    from adrt_pinv_gb300.device import Pipeline
+
+    inv = _inverses(pkg, golden)[6]
+    bs = torch.from_numpy(np.stack(_sinos(pkg, 6, 3, 70))).cuda()
+    ref = inv.pipeline(3).apply(bs).clone()
+    pipe = Pipeline(inv.plan, 3, "fp32", "cuda")
+    res = tune.Tuner(reps=1).tune(pipe, bs)
+    assert len(res["ms"]) == len(tune.candidates(pipe)) >= 2 and res["config"] in tune.candidates(pipe)
+    out = pipe.apply(bs)
+    assert float((out - ref).norm() / ref.norm()) < 1e-6

@@ -1,0 +1,48 @@
+"""Autotuner logic (candidate set, selection, cache) with a fake timer and a stand-in pipeline on the CPU."""
+import json
+import types
+
+import numpy as np
+
+
+def _pipe(torch, B, dense, real):
+    plan = types.SimpleNamespace(N=256, method="hybrid", deg_cap=32, dense_cap=16,
+                                 dense_freqs=np.arange(3) if dense else np.zeros(0))
+    tables = types.SimpleNamespace(stream_dense=False, use_tc=False, row_grid=0, _dense_dev={})
+    return types.SimpleNamespace(plan=plan, B=B, precision="fp32", real=real, device="cpu", tables=tables)
+
+
+def test_candidates_and_choice(pkg, monkeypatch, tmp_path):
+    import torch
+
+    from adrt_pinv_gb300 import tune
+
+    monkeypatch.setattr(tune, "device_info", lambda d: ("FakeGPU", 152))
+    p = _pipe(torch, 8, True, torch.float32)
+    cands = tune.candidates(p)
+    assert {c["dense"] for c in cands} == {"tc", "simt", "stream"} and {c["row_grid"] for c in cands} == {152, 304}
+    assert {c["dense"] for c in tune.candidates(_pipe(torch, 64, True, torch.float32))} == {"tc", "simt"}
+    assert {c["dense"] for c in tune.candidates(_pipe(torch, 4, False, torch.float32))} == {"none"}
+    assert {c["dense"] for c in tune.candidates(_pipe(torch, 4, True, torch.float64))} == {"simt"}
+
+    cost = {"tc": 3.0, "simt": 5.0, "stream": 2.0}
+    calls = []
+
+    def timer(pipe, b):
+        calls.append(1)
+        t = pipe.tables
+        mode = "stream" if t.stream_dense else ("tc" if t.use_tc else "simt")
+        return cost[mode] + (0.5 if t.row_grid == 304 else 0.0)
+
+    path = tmp_path / "tune.json"
+    T = tune.Tuner(path=str(path), timer=timer)
+    p.tables._dense_dev = {(0, 1, 1, 1, True): "t", (0, 1, 1, 1, False): "f"}
+    res = T.tune(p, None)
+    assert res["config"] == {"dense": "stream", "row_grid": 152}
+    assert p.tables.stream_dense and not p.tables.use_tc and p.tables.row_grid == 152
+    assert list(p.tables._dense_dev) == [(0, 1, 1, 1, True)]  # the other layout's tables are dropped
+    n = len(calls)
+    T2 = tune.Tuner(path=str(path), timer=timer)  # cached on disk: no timing
+    q = _pipe(torch, 8, True, torch.float32)
+    assert T2.tune(q, None)["config"] == res["config"] and len(calls) == n
+    assert json.load(open(path))
