@@ -1,7 +1,7 @@
 """GPU inverses (FastLpGpu / FastHybridGpu) against the reference's golden outputs and the CPU oracle.
 
 Tolerances: FP64 mode <= 1e-12 (operators) / 1e-11 (apply) relative, as the reference's own engines agree;
-FP32 mode <= 1e-5 relative error vs FP64 (the benchmark spec's bound)."""
+FP32 mode <= 1e-5 relative error vs FP64 (the accuracy target of the FP32 path)."""
 
 import numpy as np
 import pytest
