@@ -305,16 +305,27 @@ class Pipeline:
         self.st = [torch.empty((B, N, N), dtype=self.stencil_real, device=dev) for _ in range(3)]
         self.ops = _op_lists(plan)
         self.launches = 0
+        self.timer = None  # list: when set, ("pack_image" | "pack_sino" | "unpack", start, end) CUDA events per launch
 
     # ---------------------------------------------------------------- packed passes
     def _codes(self):
         return C.dtype_code(self.real)
 
+    def _timed(self, name, fn):
+        if self.timer is None:
+            fn()
+            return
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        self.timer.append((name, e0, e1))
+
     def packed_image(self, x, ops):
         """fastops._packed with strips Tq(q, E x): x (B, N, N) real on device -> self.parts."""
         p, st = self.plan, C.stream_handle()
-        C.call("adrt_pack_fft", self._codes(), p.n, self.B, 0, C.dtype_code(x.dtype), C.ptr(x), C.ptr(self.Y),
-               C.ptr(self.tables.roots), st)
+        self._timed("pack_image", lambda: C.call("adrt_pack_fft", self._codes(), p.n, self.B, 0, C.dtype_code(x.dtype),
+                                                 C.ptr(x), C.ptr(self.Y), C.ptr(self.tables.roots), st))
         self.tables.run(self.Y, ops)
         self._unpack(st)
         return self.parts
@@ -329,8 +340,9 @@ class Pipeline:
         return self.parts
 
     def _unpack(self, st):
-        C.call("adrt_ifft_unpack", self._codes(), self.plan.n, self.B, C.ptr(self.Y), C.ptr(self.parts[0]),
-               C.ptr(self.parts[1]), C.ptr(self.parts[2]), C.ptr(self.tables.roots), st)
+        self._timed("unpack", lambda: C.call("adrt_ifft_unpack", self._codes(), self.plan.n, self.B, C.ptr(self.Y),
+                                             C.ptr(self.parts[0]), C.ptr(self.parts[1]), C.ptr(self.parts[2]),
+                                             C.ptr(self.tables.roots), st))
 
     def sum_parts(self, out):
         C.call("adrt_sum3", self._codes(), self.plan.n, self.B, C.ptr(self.parts[0]), C.ptr(self.parts[1]),

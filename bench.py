@@ -200,6 +200,36 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def measured_hbm_peak():
+    """The machine's measured copy bandwidth (GB/s) from MEASURED_PEAKS.json beside this file, else the fallback."""
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured copy bandwidth (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback 6.8 TB/s"
+
+
+def hbm_rooflines(ktimer, pipe):
+    """Achieved HBM GB/s of the offset-FFT kernels in the timed region (CUDA events on their stream) against the
+    measured copy bandwidth; algorithmic bytes per launch: the image (FP64) read and the packed rows (complex64)
+    written by the image pack, the packed rows read and the three FP32 partial images written by the unpack."""
+    N, B = pipe.plan.N, pipe.B
+    isz = pipe.real.itemsize
+    y_bytes = B * (4 * N) * N * 2 * isz  # packed rows: 2L = 4N rows of N complex per image
+    bytes_ = {"pack_fft_kernel (image)": B * N * N * 8 + y_bytes,
+              "ifft_unpack_kernel": y_bytes + 3 * B * N * N * isz}
+    names = {"pack_image": "pack_fft_kernel (image)", "unpack": "ifft_unpack_kernel"}
+    peak, src = measured_hbm_peak()
+    out = {}
+    for key, label in names.items():
+        ms = [a.elapsed_time(b) for n, a, b in ktimer if n == key]
+        if ms:
+            gbs = bytes_[label] / (float(np.mean(ms)) * 1e-3) / 1e9
+            out[label] = {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                          "bytes_per_launch": bytes_[label], "launch_us": float(np.mean(ms)) * 1e3}
+    return {"kernels": out, "peak_source": src}
+
+
 def max_over_ranks(x, world, device):
     """The slowest rank's time (replicas: the job ends when the last rank ends); a no-op for one process."""
     import torch
@@ -274,6 +304,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     timer = []
     pipe.tables.timer = timer
+    ktimer = []
+    pipe.timer = ktimer
     barrier()
     torch.cuda.synchronize()
     l0 = C.load().adrt_launch_count()
@@ -292,6 +324,7 @@ def run_ours(args):
     barrier()
     launches = (C.load().adrt_launch_count() - l0) // args.steps
     pipe.tables.timer = None
+    pipe.timer = None
     ms = e0.elapsed_time(e1) / args.steps
     ms = max_over_ranks(ms, world, dev)
     value = replica_throughput(B, world, ms * 1e-3)
@@ -337,6 +370,7 @@ def run_ours(args):
             "single_image": single, "batched_over_single_image": value / world / single["eager_recon_s"],
             "e2e": {"value": e2e_value, "unit": "recon/s", "h2d_bytes_per_step": int(b_host.numel() * 8),
                     "d2h_bytes_per_step": int(out_host.numel() * 8)}}
+    line["roofline_hbm"] = hbm_rooflines(ktimer, pipe)
     if rows_launch_ms:
         achieved = flops_per_launch / (rows_launch_ms * 1e-3) / 1e12
         tr = traffic_per_launch()  # captured at N=256, batch 64; rows scale with the batch
