@@ -134,9 +134,11 @@ class _GpuInverse:
             return self._image_op(pipe, lambda x: pipe.G(x), v.reshape(N, N)).ravel()
 
         A = spla.LinearOperator((N * N, N * N), matvec=G, dtype=float)
+        # a seeded Lanczos start vector (ARPACK's default is random), so that a plan is the same on every build
+        v0 = np.random.default_rng(0).uniform(-1.0, 1.0, N * N)
         if self.method == "lp" or self.plan.precond == "none":
-            lo, ulo = spla.eigsh(A, k=1, which="SA", tol=1e-3, maxiter=300)
-            hi, uhi = spla.eigsh(A, k=1, which="LA", tol=1e-3, maxiter=300)
+            lo, ulo = spla.eigsh(A, k=1, which="SA", tol=1e-3, maxiter=300, v0=v0)
+            hi, uhi = spla.eigsh(A, k=1, which="LA", tol=1e-3, maxiter=300, v0=v0)
 
             def res(th, u):
                 return np.linalg.norm(A.matvec(u[:, 0]) - th * u[:, 0])
@@ -150,8 +152,8 @@ class _GpuInverse:
                 return pipe.precond(pipe.s).double().cpu().numpy().ravel()
 
             Minv = spla.LinearOperator((N * N, N * N), matvec=Pv, dtype=float)
-            lo, ulo = spla.eigsh(A, k=1, M=Mop, Minv=Minv, which="SA", tol=1e-3, maxiter=300)
-            hi, uhi = spla.eigsh(A, k=1, M=Mop, Minv=Minv, which="LA", tol=1e-3, maxiter=300)
+            lo, ulo = spla.eigsh(A, k=1, M=Mop, Minv=Minv, which="SA", tol=1e-3, maxiter=300, v0=v0)
+            hi, uhi = spla.eigsh(A, k=1, M=Mop, Minv=Minv, which="LA", tol=1e-3, maxiter=300, v0=v0)
 
             def res(th, u):
                 u = u[:, 0]
