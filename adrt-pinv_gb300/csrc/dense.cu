@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
     constexpr int HB = BP / 2;                                             // columns promoted per warp
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     uint64_t* mbar = reinterpret_cast<uint64_t*>(smem_raw + 2 * STAGE);
-    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 2);
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(mbar + 3);  // mbar[2]: the drain barrier of the give-up path
 
     const int r = blockIdx.x;
     const int m0 = blockIdx.y * TC_M;  // first real output row of this CTA (0 .. 2N)
@@ -198,6 +198,7 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
     if (threadIdx.x == 0) {
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[0])));
         asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[1])));
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&mbar[2])));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -330,7 +331,17 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
             promote(s);
         }
     }
-    if (!ok && threadIdx.x == 0) atomicExch(err, 1);
+    if (!ok && threadIdx.x == 0) {
+        // a wait gave up while MMAs of this CTA may still be writing its TMEM columns: before the columns are freed
+        // (and possibly handed to the next CTA on this SM), one more commit of every tcgen05 operation this thread
+        // issued goes to the spare barrier, awaited with the same bound. Flag 1: the launch's dense rows were not
+        // written; flag 2: even the drain ran out, so the stream's later device results cannot be trusted either.
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_addr(&mbar[2]))
+                     : "memory");
+        const bool drained = mbar_wait(smem_addr(&mbar[2]), 0u);
+        atomicMax(err, drained ? 1 : 2);
+    }
     if (ok) {
         const int mrow = m0 + (warp & 3) * 32 + lane;
         const int outhalf = mrow >= N ? 1 : 0;

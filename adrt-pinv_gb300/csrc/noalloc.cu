@@ -12,7 +12,9 @@
 //   * the array is kNoAllocScratchBytes = 4 MiB on every GPU that loads the library, held until the process exits;
 //     a call needs 256 + K (N/2 + 1) 16 bytes of it and is rejected (ADRT_EINVAL) above that;
 //   * the first call on a device looks up the array's device address (cudaGetSymbolAddress) with that device
-//     current; make that first call before any stream capture;
+//     current; make that first call before any stream capture. The address is cached for the life of the
+//     device's context: after cudaDeviceReset (or anything else that destroys and recreates the primary context)
+//     the cached address is stale, so a process that resets a device must not call this entry point again;
 //   * every call shares the one array and leaves its contents behind; the twiddle table is rewritten and the counter
 //     is reset (stream-ordered memset) by each call, so nothing stale is read, but two calls whose work overlaps on
 //     the GPU (different streams, no ordering between them) race on the array and give wrong results.

@@ -15,6 +15,7 @@
 //
 // Simple kernel (any n <= 11, any lo): one CTA per row, the row in shared memory in natural order, ping-pong
 // levels exactly as cpp/oblique.cpp:22-51. Used for op lists the fast kernel does not cover.
+#include <atomic>
 #include <cstdio>
 #include <type_traits>
 
@@ -767,13 +768,18 @@ __global__ void twiddle_table_kernel(int n, int K, const double2* __restrict__ z
 }
 
 // ------------------------------------------------------------------ dispatch
+// SM count of the current device, cached per device index (grids are sized for the GPU they run on)
 static int num_sms() {
-    static int sms = 0;
-    if (!sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
+    constexpr int kMaxDev = 64;
+    static std::atomic<int> cache[kMaxDev];
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= kMaxDev) dev = 0;
+    int sms = cache[dev].load(std::memory_order_relaxed);
+    if (sms <= 0) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
+        cache[dev].store(sms, std::memory_order_relaxed);
     }
     return sms;
 }

@@ -135,10 +135,13 @@ class RowTables:
     def raise_if_error(self):
         """Raise if a tensor-core dense-row launch gave up on a bounded wait since the last check (reads one int: a
         device synchronisation, so callers make it where they synchronise anyway); clears the flag."""
-        if int(self.err.item()):
+        code = int(self.err.item())
+        if code:
             self.err.zero_()
+            more = ("" if code == 1 else "; the drain of its MMAs ran out as well, so later results on this stream "
+                    "cannot be trusted")
             raise RuntimeError("dense_tc_kernel: an mbarrier wait ran out; the dense-row results of that launch "
-                               "were not written")
+                               "were not written" + more)
 
     def dense_apply(self, Y, T):
         """Y[b, r] <- T_r Y[b, r] for the dense rows (FP32: tensor cores, or the streaming CUDA-core kernel for small

@@ -24,12 +24,13 @@ from .device import Pipeline
 
 
 class Request:
-    __slots__ = ("rid", "n", "b", "t_arrival", "t_start", "t_done", "result")
+    __slots__ = ("rid", "n", "b", "t_arrival", "t_start", "t_done", "result", "error")
 
     def __init__(self, rid, n, b, t_arrival=0.0):
         self.rid, self.n, self.b, self.t_arrival = rid, n, b, t_arrival
         self.t_start = self.t_done = None
         self.result = None
+        self.error = None  # set when the batch's device work reported a failure (result is then None)
 
 
 class Lane:
@@ -62,10 +63,13 @@ class Lane:
         with torch.cuda.stream(self.stream):
             for i, r in enumerate(reqs):
                 b = r.b
-                if not (isinstance(b, torch.Tensor) and b.is_pinned() and b.dtype == torch.float64):
-                    self.stage_in[i].copy_(torch.as_tensor(np.asarray(b, dtype=np.float64)))
-                    b = self.stage_in[i]
-                self.pipe.b_in[i].copy_(b, non_blocking=True)
+                if isinstance(b, torch.Tensor):
+                    # device tensors and pinned host tensors copy straight in (copy_ casts the dtype); pageable host
+                    # tensors too, synchronously
+                    self.pipe.b_in[i].copy_(b, non_blocking=b.is_cuda or b.is_pinned())
+                    continue
+                self.stage_in[i].copy_(torch.from_numpy(np.ascontiguousarray(b, dtype=np.float64)))
+                self.pipe.b_in[i].copy_(self.stage_in[i], non_blocking=True)
             x = self.pipe.replay()
             k = len(reqs)
             self.stage_out[:k].copy_(x[:k], non_blocking=True)
@@ -77,11 +81,20 @@ class Lane:
         return self.batch is not None and self.event.query()
 
     def collect(self, keep=None):
-        """The finished batch; each request's result is copied out of the staging buffer unless keep(r) is false."""
+        """The finished batch; each request's result is copied out of the staging buffer unless keep(r) is false.
+        If the batch's tensor-core dense-row launch gave up on a bounded wait (the library's error flag, read here
+        after the completion event, so without an extra synchronisation), no result is delivered: every request
+        of the batch gets result None and its error set."""
         out = self.batch
+        self.batch = None
+        try:
+            self.pipe.tables.raise_if_error()
+        except RuntimeError as e:
+            for r in out:
+                r.result, r.error = None, str(e)
+            return out
         for i, r in enumerate(out):
             r.result = self.stage_out[i].clone() if keep is None or keep(r) else None
-        self.batch = None
         return out
 
     def release(self):

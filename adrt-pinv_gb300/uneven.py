@@ -51,9 +51,17 @@ class UnevenBatch:
             dst.copy_(src, non_blocking=True)
 
     def replay(self):
-        """One launch of the whole uneven batch on the current stream; returns the per-class result buffers."""
+        """One launch of the whole uneven batch on the current stream; returns the per-class result buffers. The
+        results are valid once the stream has reached this point and check() has passed."""
         self.graph.replay()
         return self.outputs
+
+    def check(self):
+        """Raise if a tensor-core dense-row launch of any class gave up on a bounded wait since the last check (its
+        dense rows were not written). Reads each class's error flag, a device synchronisation: call it after
+        synchronising on the replay, before the results are used."""
+        for pipe in self.pipes:
+            pipe.tables.raise_if_error()
 
     def device_bytes(self):
         return sum(p.device_bytes() for p in self.pipes)

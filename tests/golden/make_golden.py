@@ -1,8 +1,8 @@
 """Generate the golden fixtures in this directory by running the reference implementation (dsrim/adrt-pinv).
 
-Run from the repository root with the reference checked out read-only at REF (default /root/reference):
+Run from the repository root with the path of a read-only reference checkout (no default):
 
-    python tests/golden/make_golden.py [REF]
+    python tests/golden/make_golden.py REF          (or ADRT_PINV_REF=REF python tests/golden/make_golden.py)
 
 The reference is copied to a temporary directory first because its C++ engine (`fastcpp.py:19-21`) compiles
 `cpp/liboblique.so` next to its own source. Every array in the fixtures comes from the reference's own code
@@ -50,7 +50,9 @@ def _import_reference(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ADRT_PINV_REF")
+    if not ref:
+        sys.exit("usage: make_golden.py REF (the path of a reference checkout; or set ADRT_PINV_REF)")
     ac, fs, fh, fo, fc = _import_reference(ref)
     ph = _load_phantoms()
     out = {}

@@ -4,7 +4,8 @@ Some callers cannot allocate device memory: a process that has given the whole G
 must not let cudaMalloc/cudaFree synchronize the device, threads that may not enter the CUDA allocator. For them the
 library offers bfly_rows on device pointers with its scratch in a fixed device array. This checks, through the C ABI,
 two calls in a row (different sizes and directions, the second reusing the array the first left behind) against the
-regular entry point, to the FP64 tolerance of the other row-kernel tests, and that oversized calls are refused.
+regular entry point and against the reference's own outputs (golden vectors), to the FP64 tolerance of the other
+row-kernel tests, that the device's free memory does not change across calls, and that oversized calls are refused.
 Collected last on purpose, so that a failure here comes after every other test has run."""
 
 import ctypes
@@ -51,6 +52,31 @@ def test_noalloc_matches_bfly_rows_two_calls(lib):
         assert rc == 0, lib.adrt_last_error()
         torch.cuda.synchronize()
         assert max_rel(Xd.cpu().numpy(), _host_ref(lib, n, z, V, lo, hi, tr)) < 1e-12
+
+
+def test_noalloc_matches_reference_golden_and_allocates_nothing(lib, golden):
+    """Against the reference's own compiled bfly_rows (golden cpp_bfly_* vectors, cpp/oblique.cpp:56-70), two
+    calls in a row per size, and the device's free memory is the same before and after the calls (the entry point
+    allocates nothing; the first call on the device already happened in the test above or happens here, and its
+    symbol lookup allocates nothing either)."""
+    import torch
+
+    torch.cuda.synchronize()
+    for n in (4, 6):
+        V = golden[f"bf_V_{n}"]
+        z = np.ascontiguousarray(golden[f"bf_z_{n}"])
+        zd = torch.from_numpy(z).cuda()
+        cases = [(lo, hi, tr) for lo, hi in ((1, n), (2, n - 1)) for tr in (0, 1)]
+        Xs = [torch.from_numpy(np.ascontiguousarray(V)).cuda() for _ in cases]
+        torch.cuda.synchronize()
+        free0 = torch.cuda.mem_get_info()[0]
+        for (lo, hi, tr), Xd in zip(cases, Xs):
+            rc = lib.adrt_bfly_rows_noalloc(n, V.shape[0], zd.data_ptr(), Xd.data_ptr(), lo, hi, tr, None)
+            assert rc == 0, lib.adrt_last_error()
+        torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free0
+        for (lo, hi, tr), Xd in zip(cases, Xs):
+            assert max_rel(Xd.cpu().numpy(), golden[f"cpp_bfly_{n}_{lo}_{hi}_{tr}"]) < 1e-12, (n, lo, hi, tr)
 
 
 def test_noalloc_rejects_oversized_calls(lib):
