@@ -10,6 +10,7 @@ precision in fp64 mode, where everything is FP64).
 """
 
 import ctypes
+import weakref
 
 import numpy as np
 import torch
@@ -114,6 +115,11 @@ class RowTables:
         """The folded dense-row operators of one op list, one per dense packed row, in the row precision. Built on
         the host in FP64 up to n = 8 and on the device (FP64 torch, Cholesky form) for larger n."""
         key = (fold_pre, fold_post, pre_b1, post_b1t, self.stream_dense)
+        # pipelines of one plan share their tables (same device, precision and layout) while any of them holds one
+        shared = self.plan.__dict__.setdefault("_dense_shared", weakref.WeakValueDictionary())
+        skey = (str(self.device), str(self.real), key)
+        if key not in self._dense_dev and skey in shared:
+            self._dense_dev[key] = shared[skey]
         if key not in self._dense_dev:
             if self.plan.n >= 9 and self.device.type == "cuda":
                 N = self.plan.N
@@ -130,6 +136,7 @@ class RowTables:
                     T = T.transpose(0, 2, 1)
                 self._dense_dev[key] = torch.from_numpy(np.ascontiguousarray(T)).to(
                     device=self.device, dtype=_cdtype(self.real))
+            shared[skey] = self._dense_dev[key]
         return self._dense_dev[key]
 
     def raise_if_error(self):

@@ -50,6 +50,8 @@ def parse():
                          "uneven: 512 mixed N/p/method sinograms in one CUDA graph; large: N=2048, batch 1 and 8")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="batch mode: skip the short serve / uneven / large runs appended to the line")
     return ap.parse_args()
 
 
@@ -392,9 +394,37 @@ def run_ours(args):
         line["rel_err_vs_fp64"] = float(np.linalg.norm(got - ref) / np.linalg.norm(ref))
         line["cpu_baseline"] = {"value": 1.0 / t_cpu, "unit": "recon/s", "cores": threads, "kind": kind,
                                 "sample": f"one N={N} sinogram of the batch, min of 2 applies after a warm-up"}
+    if world == 1 and not args.no_extras:
+        line.update(extras(pkg, dev, args))
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def extras(pkg, dev, args):
+    """Short runs of the other workloads, appended to the batch line under their own keys (rank 0 of a one-GPU run):
+    serve (p50/p99 latency and throughput at a rate the GPU sustains and at 2000 req/s), uneven (the 512-sinogram
+    uneven batch in one CUDA graph) and large (N = 2048 at batch 1 and 8). Each reports its own accuracy against
+    FP64 and its own clocks; none is part of the headline value."""
+    import torch
+
+    out = {}
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    invs, pool, setup = serve_setup(pkg, dev)
+    runs = [serve_run(pkg, dev, invs, pool, rate, secs, seed=i)
+            for i, (rate, secs) in enumerate(((150.0, 4.0), (2000.0, 1.0)))]
+    out["serve"] = {"config": SERVE_CONFIG, "setup_s": setup, "sustained": runs[0], "at_2000_rps": runs[1],
+                    "total_s": time.perf_counter() - t0}
+    del invs, pool
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    out["uneven"] = dict(uneven_result(pkg, dev, 5, 3, tune_reps=1), config=UNEVEN_CONFIG,
+                         total_s=time.perf_counter() - t0)
+    torch.cuda.empty_cache()
+    t0 = time.perf_counter()
+    out["large"] = dict(large_result(pkg, dev, 3, 1), config=LARGE_CONFIG, total_s=time.perf_counter() - t0)
+    return out
 
 
 def _phantom_sinos(pkg, n, count, seed0, device, rel_sigma, ellipses=10, texture=0.0):
@@ -415,64 +445,81 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-def run_serve(args):
-    """Continuous batching of Poisson hybrid-inverse requests with N in {128, 256, 512, 1024} (probabilities .4, .3,
-    .2, .1), p = 32, dense_cap 16, FP32 rows with FP64 tables, 120 GB HBM budget."""
-    import torch
+SERVE_SIZES, SERVE_PROBS = [7, 8, 9, 10], [0.4, 0.3, 0.2, 0.1]
+SERVE_SLOTS = {7: 64, 8: 64, 9: 32, 10: 16}
 
-    import __graft_entry__ as ge
 
-    pkg = ge.load_package()
-    from adrt_pinv_gb300 import serve
-
-    dev = torch.device("cuda", 0)
-    sizes, probs = [7, 8, 9, 10], [0.4, 0.3, 0.2, 0.1]
-    slots = {7: 64, 8: 64, 9: 32, 10: 16}
+def serve_setup(pkg, dev):
+    """The four hybrid inverses of the serving workload (N in {128, 256, 512, 1024}, p = 32, dense_cap 16) and a pool
+    of 4 pinned noisy sinograms per size; returns (inverses, pool, setup seconds per N)."""
     setup, invs, pool = {}, {}, {}
-    for n in sizes:
+    for n in SERVE_SIZES:
         t0 = time.perf_counter()
         invs[n] = pkg.FastHybridGpu(n, deg_cap=P_CAP, dense_cap=DENSE_CAP, precision="fp32", device=dev)
         setup[1 << n] = time.perf_counter() - t0
         pool[n] = [b.cpu().pin_memory() for b in _phantom_sinos(pkg, n, 4, 500 * n, dev, REL_SIGMA)]
+    return invs, pool, setup
+
+
+def serve_run(pkg, dev, invs, pool, rate, seconds, seed=0):
+    """Continuous batching of Poisson(rate) hybrid-inverse requests for `seconds` (sizes drawn with SERVE_PROBS),
+    120 GB HBM budget; p50/p99 latency (arrival to result on the host), throughput, and the first request of each
+    size checked against the same sinogram inverted alone."""
+    from adrt_pinv_gb300 import serve
+
     check = {}
-    S = serve.InverseServer(lambda n: invs[n], lambda n: slots[n], hbm_budget_bytes=120e9, device=dev,
+    S = serve.InverseServer(lambda n: invs[n], lambda n: SERVE_SLOTS[n], hbm_budget_bytes=120e9, device=dev,
                             keep_result=lambda r: r.rid in check)
-    for n in sizes:  # lanes (graph capture) and one warm batch each, before the clock starts
+    for n in SERVE_SIZES:  # lanes (graph capture) and one warm batch each, before the clock starts
         S._admit_lane(n)
-        for i in range(slots[n]):
+        for i in range(SERVE_SLOTS[n]):
             S.submit(serve.Request(-1, n, pool[n][i % 4]))
     while S.step():
         pass
     S.finished, S.max_busy = [], 0
-    arr = serve.poisson_arrivals(args.serve_rate, args.serve_seconds, sizes, probs, seed=0)
+    arr = serve.poisson_arrivals(rate, seconds, SERVE_SIZES, SERVE_PROBS, seed=seed)
     reqs, seen = [], set()
     for i, (t, n) in enumerate(arr):
         reqs.append((t, serve.Request(i, n, pool[n][i % 4])))
         if n not in seen:  # the first request of each size is checked against the same sinogram inverted alone
             seen.add(n)
             check[i] = reqs[-1][1]
-    with ClockSampler(0) as clk:
+    with ClockSampler(dev.index or 0) as clk:
         t0 = time.perf_counter()
         done = S.run(reqs)
         wall = time.perf_counter() - t0
     st = serve.InverseServer.stats(done)
     per = {}
-    for n in sizes:
+    for n in SERVE_SIZES:
         d = [r for r in done if r.n == n]
         if d:
             per[1 << n] = serve.InverseServer.stats(d)
     same = max(_rel(r.result.numpy(), invs[r.n].apply(r.b.numpy())) for r in check.values())
-    line = {"metric": "served hybrid-inverse requests/s, mixed N (p50/p99 latency)", "value": st["throughput_rps"],
+    return {"offered_rps": len(arr) / seconds, "served_rps": st["throughput_rps"], "p50_ms": st["p50_ms"],
+            "p99_ms": st["p99_ms"], "requests": st["requests"], "arrival_seconds": seconds, "wall_s": wall,
+            "per_N": per, "max_concurrent_lanes": S.max_busy, "evictions": S.evictions,
+            "lane_device_gb": S.memory_in_use() / 1e9, "served_vs_alone_rel_err": same, "clocks": clk.summary()}
+
+
+SERVE_CONFIG = {"workload": "Poisson arrivals, N in {128,256,512,1024} w.p. {.4,.3,.2,.1}, hybrid, p=32, "
+                            "dense_cap=16, FP32 rows + FP64 tables, 120 GB HBM budget",
+                "slots": {str(1 << n): SERVE_SLOTS[n] for n in SERVE_SIZES}, "hbm_budget_gb": 120}
+
+
+def run_serve(args):
+    """The serving workload alone, at --serve-rate for --serve-seconds."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    dev = torch.device("cuda", 0)
+    invs, pool, setup = serve_setup(pkg, dev)
+    r = serve_run(pkg, dev, invs, pool, args.serve_rate, args.serve_seconds)
+    line = {"metric": "served hybrid-inverse requests/s, mixed N (p50/p99 latency)", "value": r["served_rps"],
             "unit": "req/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
             "data": "synthetic (seeded ellipse phantoms + Gaussian noise, 4 distinct sinograms per N)",
-            "config": {"workload": f"Poisson arrivals {args.serve_rate:g} req/s for {args.serve_seconds:g} s, "
-                                   "N in {128,256,512,1024} w.p. {.4,.3,.2,.1}, hybrid, p=32, dense_cap=16",
-                       "slots": {str(1 << n): slots[n] for n in sizes}, "hbm_budget_gb": 120},
-            "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"], "requests": st["requests"],
-            "offered_rps": len(arr) / args.serve_seconds, "wall_s": wall, "per_N": per,
-            "max_concurrent_lanes": S.max_busy, "evictions": S.evictions,
-            "lane_device_gb": S.memory_in_use() / 1e9, "setup_s": setup,
-            "served_vs_alone_rel_err": same, "clocks": clk.summary()}
+            "config": dict(SERVE_CONFIG, rate=args.serve_rate, seconds=args.serve_seconds), "setup_s": setup, **r}
     print(json.dumps(line), flush=True)
 
 
@@ -481,17 +528,13 @@ def run_serve(args):
 UNEVEN_DENSE_CAP = {8: None, 16: 12, 32: DENSE_CAP, 64: DENSE_CAP}
 
 
-def run_uneven(args):
+def uneven_result(pkg, dev, steps, warmup, tune_reps=3):
     """512 sinograms, N uniform in {64, 128, 256, 512}, p in {8, 16, 32, 64}, method L_p / hybrid 50/50, noise
-    sigma U[1e-4, 1e-2] max|b|, FP32 rows with FP64 tables: one CUDA graph over all 32 classes."""
+    sigma U[1e-4, 1e-2] max|b|, FP32 rows with FP64 tables: one CUDA graph over all 32 classes, every class's launch
+    configuration autotuned first; accuracy of each class's first sinogram against the FP64 pipeline."""
     import torch
 
-    import __graft_entry__ as ge
-
-    pkg = ge.load_package()
     from adrt_pinv_gb300 import inverse, tune, uneven
-
-    dev = torch.device("cuda", 0)
     rng = np.random.default_rng(2)
     total = 512
     ns = rng.choice([6, 7, 8, 9], size=total)
@@ -517,25 +560,26 @@ def run_uneven(args):
                 keys.append((n, m, p))
     setup_s = time.perf_counter() - t0
     t1 = time.perf_counter()
-    U = uneven.UnevenBatch(groups, device=dev, tuner=tune.Tuner(), sinos=sinos)
+    U = uneven.UnevenBatch(groups, device=dev, tuner=tune.Tuner(reps=tune_reps), sinos=sinos)
     tune_s = time.perf_counter() - t1
     chosen = {}
     for key, tr in zip(keys, U.tuning):
         c = tr["config"]
         chosen[f"N={1 << key[0]} {key[1]} p={key[2]}"] = f"{c['dense']}/grid{c['row_grid']}"
     U.set_inputs(sinos)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         U.replay()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with ClockSampler(0) as clk:
+    with ClockSampler(dev.index or 0) as clk:
         time.sleep(0.3)
         e0.record()
-        for _ in range(args.steps):
+        for _ in range(steps):
             U.replay()
         e1.record()
         torch.cuda.synchronize()
-    ms_step = e0.elapsed_time(e1) / args.steps
+    U.check()
+    ms_step = e0.elapsed_time(e1) / steps
     # the same classes one after another, eager (no graph, no concurrency)
     torch.cuda.synchronize()
     t1 = time.perf_counter()
@@ -548,51 +592,59 @@ def run_uneven(args):
     for key, inv, x, o in zip(keys, [g[0] for g in groups], sinos, outs):
         ref = inv.pipeline(1, "fp64").apply(x[:1].contiguous())[0].cpu().numpy()
         errs[f"N={1 << key[0]} {key[1]} p={key[2]}"] = _rel(o[0].cpu().numpy(), ref)
-    line = {"metric": "uneven-batch inverse recon/s (one CUDA graph, 32 N/p/method classes)",
-            "value": total / (ms_step * 1e-3), "unit": "recon/s", "n_gpus": 1, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic (seeded ellipse phantoms + Gaussian noise sigma U[1e-4,1e-2] max|b|)",
-            "config": {"workload": "512 sinograms, N U{64,128,256,512}, p U{8,16,32,64}, L_p/hybrid 50/50, "
-                                   "dense_cap 16 (12 at p=16, none at p=8), FP32 rows + FP64 tables", "classes": len(groups)},
-            "eager_sequential_ms": eager_ms, "graph_launches_per_step": 1, "setup_s": setup_s,
-            "autotune_s": tune_s, "autotuned": chosen,
-            "device_gb": U.device_bytes() / 1e9, "max_rel_err_vs_fp64": max(errs.values()),
-            "rel_err_vs_fp64": errs, "clocks": clk.summary()}
-    print(json.dumps(line), flush=True)
+    return {"value": total / (ms_step * 1e-3), "unit": "recon/s", "steps": steps, "warmup": warmup,
+            "ms_per_step": ms_step, "classes": len(groups), "eager_sequential_ms": eager_ms,
+            "graph_launches_per_step": 1, "setup_s": setup_s, "autotune_s": tune_s, "autotuned": chosen,
+            "device_gb": U.device_bytes() / 1e9, "max_rel_err_vs_fp64": max(errs.values()), "rel_err_vs_fp64": errs,
+            "clocks": clk.summary()}
 
 
-def run_large(args):
-    """N = 2048 (n = 11), hybrid, p = 64, dense_cap 16, FP32 rows with FP64 tables, batch 1 and 8; 40 ellipses plus
-    a 0.1-weighted uniform texture."""
+UNEVEN_CONFIG = {"workload": "512 sinograms, N U{64,128,256,512}, p U{8,16,32,64}, L_p/hybrid 50/50, "
+                             "dense_cap 16 (12 at p=16, none at p=8), FP32 rows + FP64 tables, one CUDA graph"}
+
+
+def run_uneven(args):
     import torch
 
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
-    dev = torch.device("cuda", 0)
+    r = uneven_result(pkg, torch.device("cuda", 0), args.steps, args.warmup)
+    line = {"metric": "uneven-batch inverse recon/s (one CUDA graph, 32 N/p/method classes)", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f32",
+            "data": "synthetic (seeded ellipse phantoms + Gaussian noise sigma U[1e-4,1e-2] max|b|)",
+            "config": UNEVEN_CONFIG, **r}
+    print(json.dumps(line), flush=True)
+
+
+def large_result(pkg, dev, steps, warmup, profile_region=False):
+    """N = 2048 (n = 11), hybrid, p = 64, dense_cap 16, FP32 rows with FP64 tables, batch 1 and 8; 40 ellipses plus
+    a 0.1-weighted uniform texture; relative error of the first image against the FP64 pipeline on the same plan."""
+    import torch
+
     n = 11
     t0 = time.perf_counter()
     H = pkg.FastHybridGpu(n, deg_cap=64, dense_cap=DENSE_CAP, precision="fp32", device=dev)
     setup_s = time.perf_counter() - t0
     b = _phantom_sinos(pkg, n, 8, 777, dev, REL_SIGMA, ellipses=40, texture=0.1)
     res = {}
-    with ClockSampler(0) as clk:
+    with ClockSampler(dev.index or 0) as clk:
         for B in (1, 8):
             pipe = H.pipeline(B).capture()
             x = b[:B].contiguous()
-            for _ in range(max(1, args.warmup)):
+            for _ in range(max(1, warmup)):
                 pipe.replay(x)
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            steps = max(1, min(args.steps, 5))
+            k = max(1, min(steps, 5))
             e0.record()
-            for _ in range(steps):
+            for _ in range(k):
                 pipe.replay(x)
             e1.record()
             torch.cuda.synchronize()
-            ms_b = e0.elapsed_time(e1) / steps
+            ms_b = e0.elapsed_time(e1) / k
             res[f"batch{B}"] = {"ms_per_apply": ms_b, "recon_s": B / (ms_b * 1e-3)}
-    if args.profile_region:  # one more batch-8 replay as the profiled region (per-kernel launch lists)
+    if profile_region:  # one more batch-8 replay as the profiled region (per-kernel launch lists)
         torch.cuda.synchronize()
         torch.cuda.profiler.start()
         pipe.replay(b[:8].contiguous())
@@ -600,12 +652,25 @@ def run_large(args):
         torch.cuda.profiler.stop()
     got = pipe.x_out[0].cpu().numpy()
     ref = H.pipeline(1, "fp64").apply(b[:1].contiguous())[0].cpu().numpy()
-    line = {"metric": "hybrid-inverse recon/s at N=2048 (batch 8)", "value": res["batch8"]["recon_s"],
-            "unit": "recon/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32",
-            "data": "synthetic (40 seeded ellipses + 0.1 uniform texture, noise 1e-3 max|b|)",
-            "config": {"workload": "hybrid inverse N=2048, p=64, dense_cap=16, batch 1 and 8"},
-            "results": res, "setup_s": setup_s, "outer_deg": H.outer_deg, "n_dense_freqs": H.eng.n_dense,
+    H.pipeline(8).tables.raise_if_error()
+    return {"results": res, "setup_s": setup_s, "outer_deg": H.outer_deg, "n_dense_freqs": H.eng.n_dense,
             "rel_err_vs_fp64": _rel(got, ref), "clocks": clk.summary()}
+
+
+LARGE_CONFIG = {"workload": "hybrid inverse N=2048, p=64, dense_cap=16, batch 1 and 8, FP32 rows + FP64 tables, "
+                            "40 seeded ellipses + 0.1 uniform texture, noise 1e-3 max|b|"}
+
+
+def run_large(args):
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    r = large_result(pkg, torch.device("cuda", 0), args.steps, args.warmup, args.profile_region)
+    line = {"metric": "hybrid-inverse recon/s at N=2048 (batch 8)", "value": r["results"]["batch8"]["recon_s"],
+            "unit": "recon/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": LARGE_CONFIG, **r}
     print(json.dumps(line), flush=True)
 
 
