@@ -5,7 +5,9 @@ dsrim/adrt-pinv, with every hot operation in hand-written sm_103a CUDA kernels (
     H = FastHybridGpu(8, deg_cap=32)          # plan: power iteration + Lanczos on the GPU
     x = H.apply(b)                            # b: (4, 2N-1, N) or (B, 4, 2N-1, N), NumPy or CUDA tensor
 
-Submodules: fastgpu (fastcpp drop-in), adrtcore (GPU ADRT), plan, device (pipeline), phantoms (seeded inputs).
+Submodules: fastgpu (fastcpp drop-in), adrtcore (GPU ADRT), pinv (CGLS / PCG Moore-Penrose baselines), gram (the
+row-wise normal operator and its Chebyshev least squares), plan, device (pipeline), serve (request server), uneven
+(uneven batches in one graph), tune (autotuner), phantoms (seeded inputs).
 """
 
 from . import phantoms  # noqa: F401
@@ -17,7 +19,8 @@ def __getattr__(name):
     # torch-dependent modules load on first use so that host-only tooling does not import CUDA
     import importlib
 
-    if name in ("fastgpu", "adrtcore", "device", "inverse", "stencils", "_lib", "build"):
+    if name in ("fastgpu", "adrtcore", "device", "inverse", "stencils", "_lib", "build", "pinv", "gram", "serve",
+                "uneven", "tune"):
         return importlib.import_module(f".{name}", __name__)
     if name in ("FastLpGpu", "FastHybridGpu", "power_lam_max", "cert_lam_max", "explicit_lam_max"):
         return getattr(importlib.import_module(".inverse", __name__), name)

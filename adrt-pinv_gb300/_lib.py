@@ -43,6 +43,24 @@ class RowJob(ctypes.Structure):
     ]
 
 
+class CglsState(ctypes.Structure):
+    """Mirror of `adrt_cgls` (include/adrt_pinv_gb300.h)."""
+
+    _fields_ = [("n", ctypes.c_int), ("nimg", ctypes.c_int), ("maxit", ctypes.c_int), ("nblk", ctypes.c_int),
+                ("tol", ctypes.c_double)] + [(f, ctypes.c_void_p) for f in
+                                             ("x", "p", "s", "r", "q", "scratch", "partial", "scal", "it", "active",
+                                              "hist")]
+
+
+class PcgState(ctypes.Structure):
+    """Mirror of `adrt_pcg` (include/adrt_pinv_gb300.h)."""
+
+    _fields_ = [("n", ctypes.c_int), ("nimg", ctypes.c_int), ("maxit", ctypes.c_int), ("nblk", ctypes.c_int),
+                ("tol", ctypes.c_double)] + [(f, ctypes.c_void_p) for f in
+                                             ("x", "r", "z", "p", "q", "t", "scratch", "partial", "scal", "it",
+                                              "active", "hist")]
+
+
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
@@ -71,6 +89,12 @@ PROTOTYPES = {
     "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_transpose": [_I, _I, _I, _P, _P, _P, _P],
+    "adrt_cgls_start": [ctypes.POINTER(CglsState), _P, _P],
+    "adrt_cgls_iterate": [ctypes.POINTER(CglsState), _I, _P],
+    "adrt_pcg_start": [ctypes.POINTER(PcgState), _P, _P],
+    "adrt_pcg_rho": [ctypes.POINTER(PcgState), _P],
+    "adrt_pcg_step": [ctypes.POINTER(PcgState), _P],
+    "adrt_pcg_direction": [ctypes.POINTER(PcgState), _P],
 }
 
 _lib = None

@@ -25,15 +25,18 @@ template <typename T> __device__ __forceinline__ T tq_read(const T* x, int N, in
     }
 }
 
-// one forward level for every (image, quadrant); level 1 reads T_q x, later levels read src; slot stride S elements
+// one forward level for every (image, quadrant); level 1 reads T_q x, later levels read src; slot stride S elements.
+// active (nullable): images with active[img] == 0 are skipped (their output is left as it was)
 template <typename T>
-__global__ void adrt_fwd_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S) {
+__global__ void adrt_fwd_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S,
+                               const int* __restrict__ active) {
     const int N = 1 << n, w = 1 << (m - 1);
     const int Hout = N + 2 * w - 1;
     const size_t per = (size_t)Hout * N;
     const size_t total = per * 4 * nimg;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t slot = e / per;
+        if (active && !active[slot >> 2]) continue;
         const size_t rem = e - slot * per;
         const int row = (int)(rem >> n), s = (int)(rem & (N - 1));
         const int h = row - (2 * w - 1);
@@ -68,13 +71,15 @@ template <typename T> __device__ __forceinline__ T adj_at(const T* g, int N, int
 }
 
 template <typename T>
-__global__ void adrt_adj_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S) {
+__global__ void adrt_adj_level(int n, int m, int nimg, const T* __restrict__ src, T* __restrict__ dst, size_t S,
+                               const int* __restrict__ active) {
     const int N = 1 << n, w = 1 << (m - 1);
     const int Hin = N + w - 1;
     const size_t per = (size_t)Hin * N;
     const size_t total = per * 4 * nimg;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t slot = e / per;
+        if (active && !active[slot >> 2]) continue;
         const size_t rem = e - slot * per;
         const int row = (int)(rem >> n), col = (int)(rem & (N - 1));
         dst[slot * S + rem] = adj_at(src + slot * S, N, m, row - (w - 1), col);
@@ -83,12 +88,14 @@ __global__ void adrt_adj_level(int n, int m, int nimg, const T* __restrict__ src
 
 // level-1 adjoint of the four quadrants, T_q^T and the quadrant sum (adrtcore.py:131-137)
 template <typename T>
-__global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __restrict__ x, size_t S) {
+__global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __restrict__ x, size_t S,
+                               const int* __restrict__ active) {
     const int N = 1 << n;
     const size_t per = (size_t)N * N;
     const size_t total = per * nimg;
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const size_t img = e / per;
+        if (active && !active[img]) continue;
         const size_t rem = e - img * per;
         const int a = (int)(rem >> n), b = (int)(rem & (N - 1));
         const T* g = src + img * 4 * S;
@@ -102,7 +109,7 @@ __global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __
 }
 
 template <typename T>
-static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st) {
+static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, const int* active, cudaStream_t st) {
     const int N = 1 << n;
     const size_t S = (size_t)(2 * N - 1) * N;
     T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
@@ -110,7 +117,7 @@ static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, cudaStr
     for (int m = 1; m <= n; ++m) {
         T* dst = (m == n) ? reinterpret_cast<T*>(b) : bufs[m & 1];
         const size_t total = (size_t)(N + (1 << m) - 1) * N * 4 * nimg;
-        adrt_fwd_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S);
+        adrt_fwd_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
         int rc = launch_status("adrt_fwd_level");
         if (rc) return rc;
         src = dst;
@@ -119,7 +126,7 @@ static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, cudaStr
 }
 
 template <typename T>
-static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st) {
+static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, const int* active, cudaStream_t st) {
     const int N = 1 << n;
     const size_t S = (size_t)(2 * N - 1) * N;
     T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
@@ -127,38 +134,38 @@ static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, cudaStr
     for (int m = n; m >= 2; --m) {
         T* dst = bufs[m & 1];
         const size_t total = (size_t)(N + (1 << (m - 1)) - 1) * N * 4 * nimg;
-        adrt_adj_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S);
+        adrt_adj_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
         int rc = launch_status("adrt_adj_level");
         if (rc) return rc;
         src = dst;
     }
-    adrt_adj_final<T><<<grid_of((size_t)N * N * nimg), 256, 0, st>>>(n, nimg, src, reinterpret_cast<T*>(x), S);
+    adrt_adj_final<T><<<grid_of((size_t)N * N * nimg), 256, 0, st>>>(n, nimg, src, reinterpret_cast<T*>(x), S, active);
     return launch_status("adrt_adj_final");
 }
 
-int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st) {
+int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st, const int* active) {
     if (n < 1 || n > 12 || nimg < 0) { set_error("adrt_forward: bad n=%d nimg=%d", n, nimg); return ADRT_EINVAL; }
     if (!nimg) return ADRT_OK;
     if (!x || !b || (!scratch && n > 1)) { set_error("adrt_forward: null pointer"); return ADRT_EINVAL; }
     switch (dtype) {
-        case ADRT_F32: return fwd_t<float>(n, nimg, x, b, scratch, st);
-        case ADRT_F64: return fwd_t<double>(n, nimg, x, b, scratch, st);
-        case ADRT_I32: return fwd_t<int32_t>(n, nimg, x, b, scratch, st);
-        case ADRT_I64: return fwd_t<long long>(n, nimg, x, b, scratch, st);
+        case ADRT_F32: return fwd_t<float>(n, nimg, x, b, scratch, active, st);
+        case ADRT_F64: return fwd_t<double>(n, nimg, x, b, scratch, active, st);
+        case ADRT_I32: return fwd_t<int32_t>(n, nimg, x, b, scratch, active, st);
+        case ADRT_I64: return fwd_t<long long>(n, nimg, x, b, scratch, active, st);
     }
     set_error("adrt_forward: bad dtype %d", dtype);
     return ADRT_EINVAL;
 }
 
-int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st) {
+int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st, const int* active) {
     if (n < 1 || n > 12 || nimg < 0) { set_error("adrt_transpose: bad n=%d nimg=%d", n, nimg); return ADRT_EINVAL; }
     if (!nimg) return ADRT_OK;
     if (!x || !b || (!scratch && n > 1)) { set_error("adrt_transpose: null pointer"); return ADRT_EINVAL; }
     switch (dtype) {
-        case ADRT_F32: return adj_t<float>(n, nimg, b, x, scratch, st);
-        case ADRT_F64: return adj_t<double>(n, nimg, b, x, scratch, st);
-        case ADRT_I32: return adj_t<int32_t>(n, nimg, b, x, scratch, st);
-        case ADRT_I64: return adj_t<long long>(n, nimg, b, x, scratch, st);
+        case ADRT_F32: return adj_t<float>(n, nimg, b, x, scratch, active, st);
+        case ADRT_F64: return adj_t<double>(n, nimg, b, x, scratch, active, st);
+        case ADRT_I32: return adj_t<int32_t>(n, nimg, b, x, scratch, active, st);
+        case ADRT_I64: return adj_t<long long>(n, nimg, b, x, scratch, active, st);
     }
     set_error("adrt_transpose: bad dtype %d", dtype);
     return ADRT_EINVAL;

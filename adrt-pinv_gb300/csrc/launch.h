@@ -23,8 +23,11 @@ int image_outer(int dtype, int n, int nimg, const void* x, const void* xp, const
                 double om_a, double om_1, double a0, cudaStream_t st);
 // set the dynamic shared-memory limit of a kernel once per size (safe to call before and during stream capture)
 int ensure_smem(const void* func, size_t bytes);
-int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st);
-int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st);
+// spatial ADRT levels; active (nullable): images with active[img] == 0 are skipped
+int adrt_fwd(int dtype, int n, int nimg, const void* x, void* b, void* scratch, cudaStream_t st,
+             const int* active = nullptr);
+int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, cudaStream_t st,
+             const int* active = nullptr);
 int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2, const double* x,
                const double* xp, double* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
                const double* g1_coef, cudaStream_t st);

@@ -177,6 +177,62 @@ int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, 
 int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scratch, void* stream);
 int adrt_transpose(int dtype, int n, int nimg, const void* b, void* x, void* scratch, void* stream);
 
+/* ------------------------------------------------------------------ iterative Moore-Penrose pseudoinverse
+ * pinv.py:23-48 cgls and pinv.py:51-82 pcg_normal on the GPU for nimg right-hand sides at once, FP64 throughout.
+ * The caller owns every buffer (device memory) and drives the iteration: start once, then launch blocks of
+ * iterations (or replay them from a CUDA graph) and read the per-image `active` flags between blocks; an image whose
+ * test has passed (or that reached maxit) stops changing, so every image ends with the iterate the reference's own
+ * loop returns. hist[img * (maxit + 1) + k] is the reference's history entry k (CGLS: ||R^T r_k||, PCG: ||r_k||),
+ * it[img] its last index. nblk: CTAs per image of the inner products (partial: nimg * nblk doubles), scal: nimg * 4
+ * doubles, scratch: 2 * nimg * 4 * (2N-1) * N doubles (the spatial ADRT's level buffers). */
+typedef struct adrt_cgls {
+    int n, nimg, maxit, nblk;
+    double tol;
+    double* x;       /* nimg x N x N: x0 in, the solution out */
+    double* p;       /* nimg x N x N search direction */
+    double* s;       /* nimg x N x N: R^T r */
+    double* r;       /* nimg x 4 x (2N-1) x N residual b - R x */
+    double* q;       /* nimg x 4 x (2N-1) x N: R p */
+    double* scratch;
+    double* partial;
+    double* scal;
+    int32_t* it;
+    int32_t* active;
+    double* hist;
+} adrt_cgls;
+
+/* r = b - R x, s = R^T r, p = s, gamma = <s,s>, hist[0] = sqrt(gamma) (pinv.py:26-33). b: nimg sinograms. */
+int adrt_cgls_start(const adrt_cgls* S, const double* b, void* stream);
+/* `iters` CGLS iterations (pinv.py:34-47), stream-ordered, no host synchronisation. */
+int adrt_cgls_iterate(const adrt_cgls* S, int iters, void* stream);
+
+typedef struct adrt_pcg {
+    int n, nimg, maxit, nblk;
+    double tol;
+    double* x;       /* nimg x N x N: x0 in, the solution out */
+    double* r;       /* nimg x N x N residual rhs - R^T R x */
+    double* z;       /* nimg x N x N preconditioned residual M r (may alias r: M = identity) */
+    double* p;       /* nimg x N x N search direction */
+    double* q;       /* nimg x N x N: R^T R p */
+    double* t;       /* nimg x 4 x (2N-1) x N: R p */
+    double* scratch;
+    double* partial;
+    double* scal;
+    int32_t* it;
+    int32_t* active;
+    double* hist;
+} adrt_pcg;
+
+/* r = rhs - R^T R x, hist[0] = ||r|| (pinv.py:62-69); the caller then forms z = M r and calls adrt_pcg_rho. */
+int adrt_pcg_start(const adrt_pcg* S, const double* rhs, void* stream);
+/* rho = <r, z>, p = z (pinv.py:64-66). */
+int adrt_pcg_rho(const adrt_pcg* S, void* stream);
+/* q = R^T R p, alpha = rho / <p,q>, x += alpha p, r -= alpha q, hist and the test (pinv.py:70-75); the caller then
+ * forms z = M r (for active images) and calls adrt_pcg_direction. */
+int adrt_pcg_step(const adrt_pcg* S, void* stream);
+/* rho' = <r, z>, p = z + (rho'/rho) p, rho = rho' (pinv.py:76-79). */
+int adrt_pcg_direction(const adrt_pcg* S, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
