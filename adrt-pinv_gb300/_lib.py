@@ -10,7 +10,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libadrt_pinv_gb300.so")
 
-F32, F64, I32, I64 = 0, 1, 2, 3
+F32, F64, I32, I64, F32X2 = 0, 1, 2, 3, 4
 OP_B, OP_BT, OP_M, OP_P = 0, 1, 2, 3
 MAX_OPS = 8
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported"}
@@ -84,7 +84,7 @@ PROTOTYPES = {
     "adrt_lorr": [_I, _I, _I, _P, _P, _P],
     "adrt_outer_update": [_I, _I, _I, _P, _P, _P, _I, _P, _D, _D, _D, _P],
     "adrt_sum3": [_I, _I, _I, _P, _P, _P, _P, _I, _P],
-    "adrt_outer_step": [_I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P],
+    "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P],
     "adrt_outer_step_max_n": [_I],
     "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],

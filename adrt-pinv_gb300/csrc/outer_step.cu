@@ -16,6 +16,70 @@ namespace cg = cooperative_groups;
 
 namespace adrt {
 
+// ------------------------------------------------------------------ stencil arithmetic: FP32, FP64 or float-float
+// Float-float ("double-float") numbers: an unevaluated sum hi + lo of two FP32 values with |lo| <= ulp(hi)/2, about
+// 48 significant bits, on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate). Error-free
+// transformations: TwoSum (Knuth, 6 operations, any magnitudes), Fast2Sum (Dekker, |a| >= |b|) and TwoProd through
+// one fused multiply-add; double-word sum and product as in Joldes, Muller and Popescu, "Tight and rigorous error
+// bounds for basic building blocks of double-word arithmetic", ACM TOMS 44 (2017): DWPlusDW (Algorithm 6, relative
+// error below 3u^2) and DWTimesDW (Algorithm 12, below 4u^2), u = 2^-24. Every operation is an explicitly rounded
+// intrinsic, so the compiler neither contracts nor reassociates them.
+struct ff {
+    float hi, lo;
+};
+
+__device__ __forceinline__ ff two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float ap = __fsub_rn(s, b);
+    const float bp = __fsub_rn(s, ap);
+    return {s, __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp))};
+}
+__device__ __forceinline__ ff fast_two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ ff ff_add(ff x, ff y) {
+    const ff s = two_sum(x.hi, y.hi);
+    const ff t = two_sum(x.lo, y.lo);
+    const ff v = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
+    return fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
+}
+__device__ __forceinline__ ff ff_neg(ff x) { return {-x.hi, -x.lo}; }
+__device__ __forceinline__ ff ff_mul(ff x, ff y) {
+    const float ch = __fmul_rn(x.hi, y.hi);
+    const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
+    const float tl1 = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.lo));
+    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
+    return fast_two_sum(ch, __fadd_rn(cl1, cl2));
+}
+
+// arithmetic of one stencil element type: add, sub, mul, exact scaling by powers of two, conversions from/to FP64
+template <typename T> struct StencilArith {
+    using V = T;
+    static __device__ __forceinline__ V add(V a, V b) { return a + b; }
+    static __device__ __forceinline__ V sub(V a, V b) { return a - b; }
+    static __device__ __forceinline__ V mul(V a, V b) { return a * b; }
+    static __device__ __forceinline__ V scale(V a, float p2) { return (T)p2 * a; }
+    static __device__ __forceinline__ V div12(V a) { return a / (T)12; }
+    static __device__ __forceinline__ V zero() { return (T)0; }
+    static __device__ __forceinline__ V from_d(double d) { return (T)d; }
+    static __device__ __forceinline__ double to_d(V v) { return (double)v; }
+};
+template <> struct StencilArith<ff> {
+    using V = ff;
+    static __device__ __forceinline__ V add(V a, V b) { return ff_add(a, b); }
+    static __device__ __forceinline__ V sub(V a, V b) { return ff_add(a, ff_neg(b)); }
+    static __device__ __forceinline__ V mul(V a, V b) { return ff_mul(a, b); }
+    static __device__ __forceinline__ V scale(V a, float p2) { return {p2 * a.hi, p2 * a.lo}; }  // exact
+    static __device__ __forceinline__ V div12(V a) { return ff_mul(a, from_d(1.0 / 12.0)); }
+    static __device__ __forceinline__ V zero() { return {0.f, 0.f}; }
+    static __device__ __forceinline__ V from_d(double d) {
+        const float h = __double2float_rn(d);
+        return {h, __double2float_rn(d - (double)h)};
+    }
+    static __device__ __forceinline__ double to_d(V v) { return (double)v.hi + (double)v.lo; }
+};
+
 constexpr int OS_THREADS = 512;
 constexpr int OS_MAX_STEPS = 32;
 
@@ -35,8 +99,10 @@ struct OuterStepArgs {
     double g1_om_1[OS_MAX_STEPS];
 };
 
-template <typename T, int n, int BAND>
+template <typename TS, typename TP, int n, int BAND>
 __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepArgs A) {
+    using Ar = StencilArith<TS>;
+    using T = typename Ar::V;
     constexpr int N = 1 << n;
     constexpr int CL = N / BAND;
     constexpr int E = BAND * N;  // elements per CTA
@@ -48,15 +114,15 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     T* bufA = s + E;
     T* bufB = bufA + E;
     const size_t base = (size_t)img * N * N + (size_t)rank * E;
-    const T* p0 = reinterpret_cast<const T*>(A.p0);
-    const T* p1 = reinterpret_cast<const T*>(A.p1);
-    const T* p2 = reinterpret_cast<const T*>(A.p2);
+    const TP* p0 = reinterpret_cast<const TP*>(A.p0);
+    const TP* p1 = reinterpret_cast<const TP*>(A.p1);
+    const TP* p2 = reinterpret_cast<const TP*>(A.p2);
 
-    // residual into shared memory
+    // residual into shared memory (the partial images summed in their own precision, the difference in FP64)
     for (int e = threadIdx.x; e < E; e += OS_THREADS) {
         const size_t g = base + e;
-        const T t = p0 ? (p0[g] + p1[g]) + p2[g] : (T)0;
-        s[e] = (T)(A.y[g] - (double)t);
+        const TP t = p0 ? (p0[g] + p1[g]) + p2[g] : (TP)0;
+        s[e] = Ar::from_d(A.y[g] - (double)t);
     }
     __syncthreads();
 
@@ -65,10 +131,10 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
         // x_1 = a s ; x_{k+1} = x_k + om_a (s - G1 x_k) + om_1 (x_k - x_{k-1})   (x_0 = 0)
         T* cur = bufA;
         T* prv = bufB;
-        const T a0 = (T)A.g1_a0;
+        const T a0 = Ar::from_d(A.g1_a0);
         for (int e = threadIdx.x; e < E; e += OS_THREADS) {
-            cur[e] = a0 * s[e];
-            prv[e] = (T)0;
+            cur[e] = Ar::mul(a0, s[e]);
+            prv[e] = Ar::zero();
         }
         cluster.sync();
         const T* up = rank > 0 ? cluster.map_shared_rank(bufA, rank - 1) : nullptr;     // neighbour buffers, same
@@ -79,7 +145,7 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
         constexpr int RG = OS_THREADS / CPP;                  // row-pair groups
         const int j0 = threadIdx.x % CPP, grp = threadIdx.x / CPP;
         for (int k = 1; k < A.g1_deg; ++k) {
-            const T om_a = (T)A.g1_om_a[k - 1], om_1 = (T)A.g1_om_1[k - 1];
+            const T om_a = Ar::from_d(A.g1_om_a[k - 1]), om_1 = Ar::from_d(A.g1_om_1[k - 1]);
             const ptrdiff_t off = cur - bufA;  // the current iterate lives at the same offset in every CTA
             const T* upc = up ? up + off : nullptr;
             const T* dnc = dn ? dn + off : nullptr;
@@ -99,24 +165,24 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
                     const int r0 = 2 * m, r1 = r0 + 1;
                     const T c0 = cr[r0 * N + j], c1 = cr[r1 * N + j];
                     const T q0 = cr[r0 * N + jp], q1 = cr[r1 * N + jp];
-                    const T qm = r0 > 0 ? cr[(r0 - 1) * N + jp] : (upc ? upc[(BAND - 1) * N + jp] : (T)0);
-                    const T qp = r1 < BAND - 1 ? cr[(r1 + 1) * N + jp] : (dnc ? dnc[jp] : (T)0);
-                    T b0 = (T)2 * c1, b1 = (T)2 * c0;
+                    const T qm = r0 > 0 ? cr[(r0 - 1) * N + jp] : (upc ? upc[(BAND - 1) * N + jp] : Ar::zero());
+                    const T qp = r1 < BAND - 1 ? cr[(r1 + 1) * N + jp] : (dnc ? dnc[jp] : Ar::zero());
+                    T b0 = Ar::scale(c1, 2.f), b1 = Ar::scale(c0, 2.f);
                     if (hl) {
-                        b0 += cr[r1 * N + j - 1];
-                        b1 += cr[r0 * N + j - 1];
+                        b0 = Ar::add(b0, cr[r1 * N + j - 1]);
+                        b1 = Ar::add(b1, cr[r0 * N + j - 1]);
                     }
                     if (hr) {
-                        b0 += cr[r1 * N + j + 1];
-                        b1 += cr[r0 * N + j + 1];
+                        b0 = Ar::add(b0, cr[r1 * N + j + 1]);
+                        b1 = Ar::add(b1, cr[r0 * N + j + 1]);
                     }
-                    const T a0 = ((T)2 * q0 + qm) + q1;  // K along rows (i-1 term first, then i+1)
-                    const T a1 = ((T)2 * q1 + q0) + qp;
-                    const T g0 = ((T)8 * c0 + a0) + b0;
-                    const T g1 = ((T)8 * c1 + a1) + b1;
+                    const T a0 = Ar::add(Ar::add(Ar::scale(q0, 2.f), qm), q1);  // K along rows (i-1, then i+1)
+                    const T a1 = Ar::add(Ar::add(Ar::scale(q1, 2.f), q0), qp);
+                    const T g0 = Ar::add(Ar::add(Ar::scale(c0, 8.f), a0), b0);
+                    const T g1 = Ar::add(Ar::add(Ar::scale(c1, 8.f), a1), b1);
                     const int e0 = r0 * N + j, e1 = r1 * N + j;
-                    pv[e0] = c0 + om_a * (sr[e0] - g0) + om_1 * (c0 - pv[e0]);
-                    pv[e1] = c1 + om_a * (sr[e1] - g1) + om_1 * (c1 - pv[e1]);
+                    pv[e0] = Ar::add(Ar::add(c0, Ar::mul(om_a, Ar::sub(sr[e0], g0))), Ar::mul(om_1, Ar::sub(c0, pv[e0])));
+                    pv[e1] = Ar::add(Ar::add(c1, Ar::mul(om_a, Ar::sub(sr[e1], g1))), Ar::mul(om_1, Ar::sub(c1, pv[e1])));
                 }
             }
             cluster.sync();
@@ -131,8 +197,9 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
         for (int e = threadIdx.x; e < E; e += OS_THREADS) {
             const int i = e / N, j = e - (e / N) * N;
             const int i0 = i & ~1, j0 = j & ~1;
-            const T m = ((s[i0 * N + j0] + s[i0 * N + j0 + 1]) + (s[(i0 + 1) * N + j0] + s[(i0 + 1) * N + j0 + 1])) / (T)4;
-            out[e] = (s[e] - m) / (T)4 + m / (T)12;
+            const T m = Ar::scale(Ar::add(Ar::add(s[i0 * N + j0], s[i0 * N + j0 + 1]),
+                                          Ar::add(s[(i0 + 1) * N + j0], s[(i0 + 1) * N + j0 + 1])), 0.25f);
+            out[e] = Ar::add(Ar::scale(Ar::sub(s[e], m), 0.25f), Ar::div12(m));
         }
         __syncthreads();
         r = out;
@@ -141,7 +208,7 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     // outer update in FP64
     for (int e = threadIdx.x; e < E; e += OS_THREADS) {
         const size_t g = base + e;
-        const double rv = (double)r[e];
+        const double rv = Ar::to_d(r[e]);
         if (!A.x) {
             A.xn[g] = A.a0 * rv;
         } else {
@@ -152,12 +219,12 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     }
 }
 
-template <typename T, int n, int BAND>
+template <typename TS, typename TP, int n, int BAND>
 static int launch_os_band(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     constexpr int N = 1 << n;
     constexpr int CL = N / BAND;
-    const size_t smem = 3 * (size_t)BAND * N * sizeof(T);
-    auto kern = outer_step_kernel<T, n, BAND>;
+    const size_t smem = 3 * (size_t)BAND * N * sizeof(TS);
+    auto kern = outer_step_kernel<TS, TP, n, BAND>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     if (CL > 8) {
         if (int rc = cuda_status(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
@@ -182,25 +249,47 @@ static int launch_os_band(const OuterStepArgs& A, int nimg, cudaStream_t st) {
 
 // 32-row bands; when the batch's clusters cannot fill the SMs (N <= 256), 16-row bands instead: twice the CTAs per
 // image (clusters of up to 16), half the rows each, so a small batch finishes its stencil steps sooner
-template <typename T, int n>
+template <typename TS, typename TP, int n>
 static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     constexpr int N = 1 << n;
     if constexpr (N >= 32 && N / 16 <= 16) {
-        if ((long)nimg * (N / 32) < device_sm_count()) return launch_os_band<T, n, 16>(A, nimg, st);
+        if ((long)nimg * (N / 32) < device_sm_count()) return launch_os_band<TS, TP, n, 16>(A, nimg, st);
     }
-    return launch_os_band<T, n, (N >= 32 ? 32 : N)>(A, nimg, st);
+    return launch_os_band<TS, TP, n, (N >= 32 ? 32 : N)>(A, nimg, st);
 }
 
-// largest n with a fused (cluster) outer step for element type T: the band tiles must fit 227 KB and the cluster
-// at most 16 CTAs (non-portable size above 8)
+// largest n with a fused (cluster) outer step for stencil element type dtype: the band tiles must fit 227 KB and
+// the cluster at most 16 CTAs (non-portable size above 8); 8-byte types (FP64, float-float) stop at n = 8
 int outer_step_max_n(int dtype) { return dtype == ADRT_F32 ? 9 : 8; }
 
-int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2, const double* x,
-               const double* xp, double* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
-               const double* g1_coef, cudaStream_t st) {
-    if ((dtype != ADRT_F32 && dtype != ADRT_F64) || n < 1 || n > outer_step_max_n(dtype) || nimg < 0 || precond < 0 ||
-        precond > 2 || (precond == 1 && (g1_deg < 1 || g1_deg > OS_MAX_STEPS || !g1_coef)) || (p0 && (!p1 || !p2))) {
-        set_error("outer_step: bad arguments (dtype=%d n=%d precond=%d deg=%d)", dtype, n, precond, g1_deg);
+template <typename TS, typename TP>
+static int dispatch_os(int n, const OuterStepArgs& A, int nimg, cudaStream_t st) {
+    switch (n) {
+        case 1: return launch_os<TS, TP, 1>(A, nimg, st);
+        case 2: return launch_os<TS, TP, 2>(A, nimg, st);
+        case 3: return launch_os<TS, TP, 3>(A, nimg, st);
+        case 4: return launch_os<TS, TP, 4>(A, nimg, st);
+        case 5: return launch_os<TS, TP, 5>(A, nimg, st);
+        case 6: return launch_os<TS, TP, 6>(A, nimg, st);
+        case 7: return launch_os<TS, TP, 7>(A, nimg, st);
+        case 8: return launch_os<TS, TP, 8>(A, nimg, st);
+        case 9:
+            if constexpr (sizeof(TS) == 4) return launch_os<TS, TP, 9>(A, nimg, st);
+            break;
+    }
+    set_error("outer_step: n=%d unsupported for this stencil type", n);
+    return ADRT_EUNSUPPORTED;
+}
+
+int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
+               const void* p2, const double* x, const double* xp, double* xn, double om_a, double om_1, double a0,
+               int precond, int g1_deg, const double* g1_coef, cudaStream_t st) {
+    const bool sd_ok = dtype == ADRT_F32 || dtype == ADRT_F64 || dtype == ADRT_F32X2;
+    const bool pd_ok = parts_dtype == ADRT_F32 || parts_dtype == ADRT_F64;
+    if (!sd_ok || !pd_ok || n < 1 || n > outer_step_max_n(dtype) || nimg < 0 || precond < 0 || precond > 2 ||
+        (precond == 1 && (g1_deg < 1 || g1_deg > OS_MAX_STEPS || !g1_coef)) || (p0 && (!p1 || !p2))) {
+        set_error("outer_step: bad arguments (dtype=%d parts=%d n=%d precond=%d deg=%d)", dtype, parts_dtype, n, precond,
+                  g1_deg);
         return ADRT_EINVAL;
     }
     if (!nimg) return ADRT_OK;
@@ -215,31 +304,16 @@ int outer_step(int dtype, int n, int nimg, const double* y, const void* p0, cons
             A.g1_om_1[k - 1] = g1_coef[2 * k];
         }
     }
-    if (dtype == ADRT_F32) {
-        switch (n) {
-            case 1: return launch_os<float, 1>(A, nimg, st);
-            case 2: return launch_os<float, 2>(A, nimg, st);
-            case 3: return launch_os<float, 3>(A, nimg, st);
-            case 4: return launch_os<float, 4>(A, nimg, st);
-            case 5: return launch_os<float, 5>(A, nimg, st);
-            case 6: return launch_os<float, 6>(A, nimg, st);
-            case 7: return launch_os<float, 7>(A, nimg, st);
-            case 8: return launch_os<float, 8>(A, nimg, st);
-            case 9: return launch_os<float, 9>(A, nimg, st);
-        }
-    } else {
-        switch (n) {
-            case 1: return launch_os<double, 1>(A, nimg, st);
-            case 2: return launch_os<double, 2>(A, nimg, st);
-            case 3: return launch_os<double, 3>(A, nimg, st);
-            case 4: return launch_os<double, 4>(A, nimg, st);
-            case 5: return launch_os<double, 5>(A, nimg, st);
-            case 6: return launch_os<double, 6>(A, nimg, st);
-            case 7: return launch_os<double, 7>(A, nimg, st);
-            case 8: return launch_os<double, 8>(A, nimg, st);
+    // instantiated pairs: FP32 partial images with any stencil type, FP64 partial images with the FP64 stencil
+    if (parts_dtype == ADRT_F32) {
+        switch (dtype) {
+            case ADRT_F32: return dispatch_os<float, float>(n, A, nimg, st);
+            case ADRT_F64: return dispatch_os<double, float>(n, A, nimg, st);
+            default: return dispatch_os<ff, float>(n, A, nimg, st);
         }
     }
-    set_error("outer_step: n=%d unsupported", n);
+    if (dtype == ADRT_F64) return dispatch_os<double, double>(n, A, nimg, st);
+    set_error("outer_step: FP64 partial images take the FP64 stencil only");
     return ADRT_EUNSUPPORTED;
 }
 

@@ -20,6 +20,10 @@ from .plan import Plan, outer_coeffs, roots_of_unity
 
 OPCODE = {"B": C.OP_B, "BT": C.OP_BT, "M": C.OP_M, "P": C.OP_P}
 PRECISIONS = {"fp32": torch.float32, "fp64": torch.float64}
+# the cross-quadrant preconditioner's precision: "ff" is float-float (pairs of FP32, about 48 significant bits) in the
+# fused outer step, with FP64 buffers for the separate stencil kernels where the fused step does not apply
+STENCIL_PRECISIONS = {"fp32": torch.float32, "fp64": torch.float64, "ff": torch.float64}
+STENCIL_CODES = {"fp32": C.F32, "fp64": C.F64, "ff": C.F32X2}
 
 
 def fuse_ops(ops):
@@ -302,7 +306,11 @@ class Pipeline:
         self.device = torch.device(device)
         self.real = PRECISIONS[precision]
         self.outer_real = torch.float64
-        self.stencil_real = PRECISIONS[stencil_precision or precision]
+        self.stencil_precision = stencil_precision or precision
+        if self.stencil_precision not in STENCIL_PRECISIONS:
+            raise ValueError(f"stencil_precision must be one of {tuple(STENCIL_PRECISIONS)}")
+        self.stencil_real = STENCIL_PRECISIONS[self.stencil_precision]
+        self.stencil_code = STENCIL_CODES[self.stencil_precision]
         self.tables = RowTables(plan, self.real, self.device)
         self.tables.stream_dense = self.real == torch.float32 and self.B <= 16
         N, L, B = plan.N, plan.L, self.B
@@ -390,7 +398,10 @@ class Pipeline:
         return bufs[cur]
 
     def fused_outer_ok(self):
-        return self.plan.n <= C.load().adrt_outer_step_max_n(C.dtype_code(self.stencil_real))
+        """The fused outer step exists for this size and pairing (FP32 rows with any stencil precision, FP64 rows
+        with the FP64 stencil)."""
+        pair = self.real == torch.float32 or self.stencil_precision == "fp64"
+        return pair and self.plan.n <= C.load().adrt_outer_step_max_n(self.stencil_code)
 
     def fused_outer_step(self, y, with_parts, x, x_prev, x_new, om_a, om_1, a0):
         """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step)."""
@@ -402,7 +413,7 @@ class Pipeline:
         else:
             coef = np.zeros(1)
         parts = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
-        C.call("adrt_outer_step", C.dtype_code(self.stencil_real), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
+        C.call("adrt_outer_step", self.stencil_code, self._codes(), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
                C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
                p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.stream_handle())
 
@@ -438,7 +449,7 @@ class Pipeline:
         backprojection) and the dense-row staging, computed without allocating anything."""
         N, L, B = plan.N, plan.L, int(batch)
         rs = PRECISIONS[precision].itemsize
-        ss = PRECISIONS[stencil_precision or precision].itemsize
+        ss = STENCIL_PRECISIONS[stencil_precision or precision].itemsize
         nd = 2 * len(plan.dense_freqs)
         img = B * N * N
         total = B * 2 * L * N * 2 * rs + 3 * img * rs + 4 * img * 8 + 4 * img * ss
@@ -484,7 +495,7 @@ class Pipeline:
         a, c, steps = outer_coeffs(p.lo, p.hi, p.outer_deg)
         y = self.backproject_into(b, self.y)
         hybrid = p.method == "hybrid"
-        fused = self.fused_outer_ok() and self.parts.dtype == self.stencil_real
+        fused = self.fused_outer_ok()
         x, xp = self.xs[0], None
         if fused:
             self.fused_outer_step(y, False, None, None, x, 0.0, 0.0, a)

@@ -30,6 +30,7 @@ extern "C" {
 #define ADRT_F64 1
 #define ADRT_I32 2
 #define ADRT_I64 3
+#define ADRT_F32X2 4 /* float-float: the unevaluated sum of two FP32 values, about 48 significant bits (stencils) */
 
 /* row-program operations (the op lists of fastops.RowEngine.run, fastops.py:156-167) */
 #define ADRT_OP_B 0  /* forward butterflies B_hi ... B_lo */
@@ -151,14 +152,16 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
               void* stream);
 
 /* One fused outer step (fastops._outer, fastops.py:247-258, with P of fasthybrid.py:101-130):
- *   s = y - (p0 + p1 + p2) (parts in dtype, all NULL: s = y);  r = P s  (precond 0: identity, 1: g1_inv with
- *   g1_deg steps, 2: lorr_inv);  x_new = x + om_a r + om_1 (x - x_prev)  (x == NULL: x_new = a0 r; x_prev NULL: 0).
- * y, x, x_prev, x_new are FP64; s and the stencil iterates are dtype. One thread-block cluster per image keeps the
+ *   s = y - (p0 + p1 + p2) (parts in parts_dtype, F32 or F64; all NULL: s = y);  r = P s  (precond 0: identity,
+ *   1: g1_inv with g1_deg steps, 2: lorr_inv);  x_new = x + om_a r + om_1 (x - x_prev)  (x == NULL: x_new = a0 r;
+ *   x_prev NULL: 0).
+ * y, x, x_prev, x_new are FP64; s and the stencil iterates are dtype (F32, F64 or F32X2, float-float on the FP32
+ * pipe). One thread-block cluster per image keeps the
  * image in shared memory for every stencil step. g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
  * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). Supported: n <= adrt_outer_step_max_n(dtype). */
-int adrt_outer_step(int dtype, int n, int nimg, const double* y, const void* p0, const void* p1, const void* p2,
-                    const double* x, const double* x_prev, double* x_new, double om_a, double om_1, double a0,
-                    int precond, int g1_deg, const double* g1_coef, void* stream);
+int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
+                    const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
+                    double a0, int precond, int g1_deg, const double* g1_coef, void* stream);
 int adrt_outer_step_max_n(int dtype);
 
 /* Dense low-frequency rows (fastops.py:28-40, 100-117): for r < nrows and every image b,

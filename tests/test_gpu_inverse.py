@@ -189,3 +189,32 @@ def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond, nimg):
     r = pipe.precond(pipe.resid(y, with_parts=False)) if method == "hybrid" else y
     pipe.outer_step(None, None, r, out_s, 0.0, 0.0, 0.25)
     assert (out_f - out_s).abs().max().item() / out_s.abs().max().item() < tol
+
+
+@pytest.mark.parametrize("sprec,tol", [("fp64", 1e-12), ("ff", 1e-10)])
+@pytest.mark.parametrize("n,nimg", [(4, 2), (6, 3), (8, 3), (8, 40)])
+def test_fused_cross_quadrant_inverse_high_precision(pkg, sprec, tol, n, nimg):
+    """The fused outer step of an FP32 pipeline with the cross-quadrant preconditioner in FP64 or float-float:
+    x_new = a0 g1_inv(y) against the oracle's g1_inv (fasthybrid.py:114-130, pinned to the reference's golden
+    values) image by image; FP64 to 1e-12, float-float to 1e-10. With FP32 partial images the residual is
+    y - (p0 + p1 + p2) summed in FP32 and differenced in FP64, checked on the same images."""
+    import torch
+
+    N = 1 << n
+    plan = pkg.Plan("hybrid", n, np.full(2 * N, 4.0), precond="g1", outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, nimg, "fp32", stencil_precision=sprec)
+    assert pipe.fused_outer_ok()
+    rng = np.random.default_rng(n + nimg)
+    y = rng.standard_normal((nimg, N, N))
+    out = torch.empty((nimg, N, N), dtype=torch.float64, device="cuda")
+    pipe.fused_outer_step(torch.from_numpy(y).cuda(), False, None, None, out, 0.0, 0.0, 0.5)
+    got = out.cpu().numpy()
+    for i in range(nimg):
+        assert rel_err(got[i], 0.5 * O.g1_inv(y[i])) < tol
+    pipe.parts.normal_()
+    pipe.fused_outer_step(torch.from_numpy(y).cuda(), True, None, None, out, 0.0, 0.0, 1.0)
+    parts = pipe.parts.cpu().numpy()
+    s = y - ((parts[0] + parts[1]) + parts[2]).astype(np.float64)
+    got = out.cpu().numpy()
+    for i in range(min(nimg, 3)):
+        assert rel_err(got[i], O.g1_inv(s[i])) < tol
