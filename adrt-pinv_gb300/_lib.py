@@ -84,7 +84,7 @@ PROTOTYPES = {
     "adrt_lorr": [_I, _I, _I, _P, _P, _P],
     "adrt_outer_update": [_I, _I, _I, _P, _P, _P, _I, _P, _D, _D, _D, _P],
     "adrt_sum3": [_I, _I, _I, _P, _P, _P, _P, _I, _P],
-    "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P],
+    "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _P],
     "adrt_outer_step_max_n": [_I],
     "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],

@@ -273,9 +273,9 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
 
 int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                     const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
-                    double a0, int precond, int g1_deg, const double* g1_coef, void* stream) {
+                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, void* stream) {
     return outer_step(dtype, parts_dtype, n, nimg, y, p0, p1, p2, x, x_prev, x_new, om_a, om_1, a0, precond, g1_deg,
-                      g1_coef, as_stream(stream));
+                      g1_coef, om_img, as_stream(stream));
 }
 
 int adrt_outer_step_max_n(int dtype) { return outer_step_max_n(dtype); }

@@ -92,6 +92,7 @@ struct OuterStepArgs {
     const double* xp;
     double* xn;
     double om_a, om_1, a0;
+    const double* om_img;  // nullable: per-image (om_a, om_1) pairs replacing om_a, om_1 (slot-level serving)
     int precond;  // 0 none, 1 g1, 2 lorr
     int g1_deg;
     double g1_a0;
@@ -206,6 +207,8 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     }
 
     // outer update in FP64
+    const double oa = A.om_img ? A.om_img[2 * img] : A.om_a;
+    const double o1 = A.om_img ? A.om_img[2 * img + 1] : A.om_1;
     for (int e = threadIdx.x; e < E; e += OS_THREADS) {
         const size_t g = base + e;
         const double rv = Ar::to_d(r[e]);
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
         } else {
             const double xv = A.x[g];
             const double prev = A.xp ? A.xp[g] : 0.0;
-            A.xn[g] = xv + A.om_a * rv + A.om_1 * (xv - prev);
+            A.xn[g] = xv + oa * rv + o1 * (xv - prev);
         }
     }
 }
@@ -283,7 +286,7 @@ static int dispatch_os(int n, const OuterStepArgs& A, int nimg, cudaStream_t st)
 
 int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                const void* p2, const double* x, const double* xp, double* xn, double om_a, double om_1, double a0,
-               int precond, int g1_deg, const double* g1_coef, cudaStream_t st) {
+               int precond, int g1_deg, const double* g1_coef, const double* om_img, cudaStream_t st) {
     const bool sd_ok = dtype == ADRT_F32 || dtype == ADRT_F64 || dtype == ADRT_F32X2;
     const bool pd_ok = parts_dtype == ADRT_F32 || parts_dtype == ADRT_F64;
     if (!sd_ok || !pd_ok || n < 1 || n > outer_step_max_n(dtype) || nimg < 0 || precond < 0 || precond > 2 ||
@@ -293,10 +296,10 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
         return ADRT_EINVAL;
     }
     if (!nimg) return ADRT_OK;
-    if (!y || !xn) { set_error("outer_step: null pointer"); return ADRT_EINVAL; }
+    if (!y || !xn || (om_img && !x)) { set_error("outer_step: null pointer"); return ADRT_EINVAL; }
     OuterStepArgs A = {};
     A.y = y; A.p0 = p0; A.p1 = p1; A.p2 = p2; A.x = x; A.xp = xp; A.xn = xn;
-    A.om_a = om_a; A.om_1 = om_1; A.a0 = a0; A.precond = precond; A.g1_deg = g1_deg;
+    A.om_a = om_a; A.om_1 = om_1; A.a0 = a0; A.om_img = om_img; A.precond = precond; A.g1_deg = g1_deg;
     if (precond == 1) {
         A.g1_a0 = g1_coef[0];
         for (int k = 1; k < g1_deg; ++k) {

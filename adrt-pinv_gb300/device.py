@@ -403,8 +403,9 @@ class Pipeline:
         pair = self.real == torch.float32 or self.stencil_precision == "fp64"
         return pair and self.plan.n <= C.load().adrt_outer_step_max_n(self.stencil_code)
 
-    def fused_outer_step(self, y, with_parts, x, x_prev, x_new, om_a, om_1, a0):
-        """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step)."""
+    def fused_outer_step(self, y, with_parts, x, x_prev, x_new, om_a, om_1, a0, om_img=None):
+        """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step); om_img (device
+        (B, 2) FP64, optional): per-image (om_a, om_1)."""
         p = self.plan
         pc = {"none": 0, "g1": 1, "lorr": 2}[p.precond] if p.method == "hybrid" else 0
         if pc == 1:
@@ -415,7 +416,7 @@ class Pipeline:
         parts = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
         C.call("adrt_outer_step", self.stencil_code, self._codes(), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
                C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
-               p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.stream_handle())
+               p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), C.stream_handle())
 
     def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0):
         C.call("adrt_outer_update", C.dtype_code(x_new.dtype), self.plan.n, self.B, C.ptr(x), C.ptr(x_prev), C.ptr(r),

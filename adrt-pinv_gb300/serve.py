@@ -1,14 +1,22 @@
 """Continuous-batching request server for the GPU inverses.
 
-Requests (one sinogram each, of any supported N) queue per size. Each size has a lane: a device pipeline with a fixed
-number of slots (its batch) captured in a CUDA graph, on its own CUDA stream, so batches of different sizes run
-concurrently on the GPU. Whenever a lane is idle and requests of its size wait, up to `slots` of them are packed into
-its pinned staging buffer, copied in, the graph is replayed and the results are copied back, all stream-ordered; the
-lane is busy until its completion event fires, and requests that arrive meanwhile are admitted into the next batch
-as soon as the slots free up (a batch never waits to fill). A lane for a new size is created only if its device
-memory (estimated before anything is allocated) fits the HBM budget beside the lanes that exist; idle lanes with no
-waiting requests are evicted, least recently used first, to make room, and otherwise the new size waits. A batch's
-state (sinograms, packed rows, iterates) stays on the device for its whole inverse.
+Requests (one sinogram each, of any supported N) queue per size. Each size has a lane on its own CUDA stream, so the
+lanes of different sizes run concurrently on the GPU. Two kinds of lane:
+
+  SlotLane (the default, slot-level batching): a pipeline of B slots that advances one outer Chebyshev step at a
+    time for all slots together, each slot at its own outer iteration (per-slot coefficients on the device). A
+    request is admitted into any free slot between two steps: its sinogram is back-projected into the slot (a
+    batch-1 pipeline on the lane's stream) and the slot's iterates are cleared; after D steps its result is copied
+    out and the slot is free again. So a request never waits for another request's whole inverse, only for one
+    step (about D times shorter), and requests of one size overlap on the device at different iterations. Each
+    step is a CUDA graph (one per phase of the three rotating iterate buffers).
+  Lane (batch-level): the whole inverse of up to B requests as one CUDA graph; new requests wait until the batch in
+    flight has finished.
+
+A lane for a new size is created only if its device memory (estimated before anything is allocated) fits the HBM
+budget beside the lanes that exist; idle lanes with no waiting requests are evicted, least recently used first, to
+make room, and otherwise the new size waits. A request's state (sinogram, packed rows, iterates) stays on the device
+for its whole inverse.
 
 make_inverse(n) builds (or loads) the inverse of size 2^n; its plan setup runs on the first request of that size,
 so a caller that cannot afford it in the request path builds the inverses before serving.
@@ -21,6 +29,7 @@ import numpy as np
 import torch
 
 from .device import Pipeline
+from .plan import outer_coeffs
 
 
 class Request:
@@ -101,14 +110,189 @@ class Lane:
         """Drop the captured graph and the pipeline's buffers."""
         self.pipe = None
 
+    # the server's lane interface
+    def free_slots(self):
+        return self.slots if self.batch is None else 0
+
+    def admit(self, reqs):
+        self.launch(reqs)
+
+    def poll(self, keep=None):
+        return self.collect(keep) if self.done() else []
+
+    def advance(self):
+        pass
+
+    def in_flight(self):
+        return len(self.batch) if self.batch else 0
+
+
+class SlotLane:
+    """One size with slot-level batching: `slots` images step through the outer Chebyshev iteration together, each
+    at its own iteration k (0 .. D); a slot at k = D is free (its iterate is frozen: both per-slot coefficients
+    are zero). The step is x_{k+1} = x_k + om_a(k) P(y - G x_k) + om_1(k) (x_k - x_{k-1}) with x_0 = x_{-1} = 0 and
+    (om_a(0), om_1(0)) = (a, 0), the reference's outer loop (fastops.py:247-258) written uniformly, so that a slot
+    admitted between two steps starts at k = 0 while the others go on."""
+
+    def __init__(self, inverse, slots, device):
+        self.inv, self.slots = inverse, int(slots)
+        self.N = N = inverse.N
+        plan = inverse.plan
+        self.D = D = int(plan.outer_deg)
+        self.device = torch.device(device)
+        self.stream = torch.cuda.Stream(device=self.device)
+        with torch.cuda.stream(self.stream):
+            self.pipe = Pipeline(plan, self.slots, inverse.precision, self.device, inverse.stencil_precision)
+            self.bp = Pipeline(plan, 1, inverse.precision, self.device, inverse.stencil_precision)
+            a, _, steps = outer_coeffs(plan.lo, plan.hi, D)
+            tab = [(a, 0.0)] + [tuple(st) for st in steps] + [(0.0, 0.0)]
+            self.coef_tab = torch.tensor(tab, dtype=torch.float64, device=self.device)  # row D: a frozen slot
+            self.k = torch.full((self.slots,), D, dtype=torch.int64, device=self.device)
+            self.om = torch.zeros((self.slots, 2), dtype=torch.float64, device=self.device)
+            for x in self.pipe.xs:
+                x.zero_()
+            self.pipe.y.zero_()
+            self.b1 = torch.zeros((1, 4, 2 * N - 1, N), dtype=torch.float64, device=self.device)
+            self._step_eager(0)  # builds every table and kernel attribute before the capture
+            self._step_eager(1)
+            self.bp.backproject_into(self.b1, self.pipe.y[:1])
+            self.pipe.y.zero_()
+        self.stream.synchronize()
+        self.graphs = []
+        for ph in range(3):
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=self.stream):
+                self._step_eager(ph)
+            self.graphs.append(g)
+        self.s = 0  # global step counter (the buffer rotation phase is s % 3)
+        self.hk = [D] * self.slots  # host mirror of the per-slot iteration counters
+        self.req = [None] * self.slots
+        self.stage_in = torch.zeros((1, 4, 2 * N - 1, N), dtype=torch.float64, pin_memory=True)
+        self.stage_out = torch.empty((self.slots, N, N), dtype=torch.float64, pin_memory=True)
+        self.out_events = []  # (slot, request, event) of result copies in flight
+        self.step_events = deque()  # completion events of the steps in flight (at most `depth`)
+        self.depth = 2  # steps queued ahead: the GPU never waits for the host, an admission waits at most 2 steps
+        self.steps_run = 0
+
+    @staticmethod
+    def estimate_bytes(inverse, slots):
+        """The slot pipeline, the batch-1 back-projection pipeline and the per-slot coefficient state."""
+        p = inverse.plan
+        return (Pipeline.estimate_bytes(p, slots, inverse.precision, inverse.stencil_precision, captured=False) +
+                Pipeline.estimate_bytes(p, 1, inverse.precision, inverse.stencil_precision, captured=True) +
+                int(slots) * 24 + (int(p.outer_deg) + 1) * 16)
+
+    def device_bytes(self):
+        return (self.pipe.device_bytes() + self.bp.device_bytes() + self.b1.numel() * 8 + self.k.numel() * 8 +
+                self.om.numel() * 8 + self.coef_tab.numel() * 8)
+
+    def _bufs(self, ph):
+        xs = self.pipe.xs
+        return xs[ph % 3], xs[(ph + 2) % 3], xs[(ph + 1) % 3]  # cur, prev, new
+
+    def _step_eager(self, ph):
+        cur, prev, new = self._bufs(ph)
+        torch.index_select(self.coef_tab, 0, self.k, out=self.om)
+        self.pipe.G(cur)
+        self.pipe.fused_outer_step(self.pipe.y, True, cur, prev, new, 0.0, 0.0, 0.0, om_img=self.om)
+        self.k.add_(1).clamp_(max=self.D)
+
+    # the server's lane interface
+    def free_slots(self):
+        return sum(1 for r in self.req if r is None)
+
+    def in_flight(self):
+        return sum(1 for r in self.req if r is not None) + len(self.out_events)
+
+    def admit(self, reqs):
+        """Each request into a free slot, stream-ordered before the next step: its sinogram back-projected into the
+        slot's y, the slot's two live iterates cleared, its counter set to 0."""
+        free = [i for i, r in enumerate(self.req) if r is None]
+        assert len(reqs) <= len(free)
+        cur, prev, _ = self._bufs(self.s)
+        with torch.cuda.stream(self.stream):
+            for i, r in zip(free, reqs):
+                b = r.b
+                if isinstance(b, torch.Tensor):
+                    self.b1[0].copy_(b, non_blocking=b.is_cuda or b.is_pinned())
+                else:
+                    self.stage_in[0].copy_(torch.from_numpy(np.ascontiguousarray(b, dtype=np.float64)))
+                    self.b1.copy_(self.stage_in, non_blocking=True)
+                self.bp.backproject_into(self.b1, self.pipe.y[i:i + 1])
+                cur[i].zero_()
+                prev[i].zero_()
+                self.k[i:i + 1].fill_(0)
+                self.req[i] = r
+                self.hk[i] = 0
+
+    def advance(self):
+        """Queue the next step while some slot is active and fewer than `depth` steps are in flight; the results
+        of slots that reach k = D are copied out right after their last step."""
+        if not any(r is not None for r in self.req):
+            return
+        while self.step_events and self.step_events[0].query():
+            self.step_events.popleft()
+        if len(self.step_events) >= self.depth:
+            return
+        with torch.cuda.stream(self.stream):
+            self.graphs[self.s % 3].replay()
+            _, _, new = self._bufs(self.s)
+            self.s += 1
+            self.steps_run += 1
+            for i, r in enumerate(self.req):
+                if r is None:
+                    continue
+                self.hk[i] += 1
+                if self.hk[i] == self.D:
+                    self.stage_out[i].copy_(new[i], non_blocking=True)
+                    ev = torch.cuda.Event()
+                    ev.record(self.stream)
+                    self.out_events.append((i, r, ev))
+                    self.req[i] = None
+            ev = torch.cuda.Event()
+            ev.record(self.stream)
+            self.step_events.append(ev)
+
+    def poll(self, keep=None):
+        """Requests whose result copies have completed (device error flags checked first)."""
+        done, rest = [], []
+        for i, r, ev in self.out_events:
+            if ev.query():
+                done.append((i, r))
+            else:
+                rest.append((i, r, ev))
+        self.out_events = rest
+        if not done:
+            return []
+        err = None
+        try:
+            self.pipe.tables.raise_if_error()
+            self.bp.tables.raise_if_error()
+        except RuntimeError as e:
+            err = str(e)
+        out = []
+        for i, r in done:
+            if err is not None:
+                r.result, r.error = None, err
+            else:
+                r.result = self.stage_out[i].clone() if keep is None or keep(r) else None
+            out.append(r)
+        return out
+
+    def release(self):
+        self.graphs = []
+        self.pipe = self.bp = None
+
 
 class InverseServer:
     """make_inverse(key) -> FastHybridGpu / FastLpGpu for a request key (its size n, or any hashable class such as
     (n, method, p)); slots(key) -> batch slots of that key's lane. Request.n holds the key."""
 
-    lane_cls = Lane
+    lane_cls = SlotLane
 
-    def __init__(self, make_inverse, slots, hbm_budget_bytes=120e9, device="cuda", keep_result=None):
+    def __init__(self, make_inverse, slots, hbm_budget_bytes=120e9, device="cuda", keep_result=None, lane_cls=None):
+        if lane_cls is not None:
+            self.lane_cls = lane_cls
         self.make_inverse, self.slots, self.budget = make_inverse, slots, float(hbm_budget_bytes)
         self.keep_result = keep_result  # keep_result(request) -> bool; None keeps every result
         self.device = torch.device(device)
@@ -132,7 +316,8 @@ class InverseServer:
         need = self.lane_cls.estimate_bytes(inv, self.slots(n))
         if need > self.budget:
             raise MemoryError(f"a lane for n={n} needs {need} bytes, above the budget of {self.budget:.0f}")
-        victims = sorted((self.last_used[m], m) for m, l in self.lanes.items() if l.batch is None and not self.queues.get(m))
+        victims = sorted((self.last_used.get(m, 0.0), m) for m, l in self.lanes.items()
+                         if not l.in_flight() and not self.queues.get(m))
         while self.memory_in_use() + need > self.budget and victims:
             _, m = victims.pop(0)
             self.lanes.pop(m).release()
@@ -146,30 +331,36 @@ class InverseServer:
         self.queues.setdefault(req.n, deque()).append(req)
 
     def pending(self):
-        return sum(len(q) for q in self.queues.values()) + sum(len(l.batch) for l in self.lanes.values() if l.batch)
+        return sum(len(q) for q in self.queues.values()) + sum(l.in_flight() for l in self.lanes.values())
 
     def step(self):
-        """Collect finished batches and start new ones on idle lanes; returns the number of requests waiting or
-        in flight."""
+        """Collect finished requests, admit waiting ones into free slots, advance the lanes; returns the number of
+        requests waiting or in flight."""
         for n, lane in self.lanes.items():
-            if lane.done():
+            got = lane.poll(self.keep_result)
+            if got:
                 t = self.clock()
-                for r in lane.collect(self.keep_result):
+                for r in got:
                     r.t_done = t
                     self.finished.append(r)
         for n, q in self.queues.items():
             if not q:
                 continue
             lane = self._admit_lane(n)
-            if lane is None or lane.batch is not None:
+            if lane is None:
                 continue
-            take = [q.popleft() for _ in range(min(lane.slots, len(q)))]
+            k = min(lane.free_slots(), len(q))
+            if not k:
+                continue
+            take = [q.popleft() for _ in range(k)]
             t = self.clock()
             for r in take:
                 r.t_start = t
-            lane.launch(take)
+            lane.admit(take)
             self.last_used[n] = t
-        self.max_busy = max(self.max_busy, sum(1 for l in self.lanes.values() if l.batch is not None))
+        for lane in self.lanes.values():
+            lane.advance()
+        self.max_busy = max(self.max_busy, sum(1 for l in self.lanes.values() if l.in_flight()))
         return self.pending()
 
     def run(self, arrivals, poll_sleep=5e-5):

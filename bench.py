@@ -32,6 +32,7 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 N_LOG2, BATCH, P_CAP, DENSE_CAP, REL_SIGMA = 8, 64, 32, 16, 1e-3
+STENCIL = "ff"  # the cross-quadrant explicit inverse in FP64-class (float-float) arithmetic
 METRIC = "hybrid-inverse recon/s at N=256 (<=1e-5 vs FP64)"
 
 
@@ -50,9 +51,14 @@ def parse():
                          "uneven: 512 mixed N/p/method sinograms in one CUDA graph; large: N=2048, batch 1 and 8")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--serve-rate", type=float, default=2000.0)
+    ap.add_argument("--stencil", default=STENCIL, choices=["fp32", "ff", "fp64"],
+                    help="precision of the cross-quadrant preconditioner (ff: float-float, about 48 bits)")
     ap.add_argument("--no-extras", action="store_true",
                     help="batch mode: skip the short serve / uneven / large runs appended to the line")
     return ap.parse_args()
+
+
+STENCIL_NAMES = {"fp32": "fp32", "ff": "float-float (fp64-class)", "fp64": "fp64"}
 
 
 def config(args, world):
@@ -60,7 +66,9 @@ def config(args, world):
     return {"workload": f"hybrid inverse, N={N}, batch {args.batch} per GPU, p={P_CAP}, dense_cap={DENSE_CAP}, "
                         f"10-ellipse phantoms + noise {REL_SIGMA:g} max|b|",
             "N": N, "global_batch": args.batch * world, "p": P_CAP, "dense_cap": DENSE_CAP, "method": "hybrid",
-            "precond": "g1", "precision": "fp32 rows/FFT/stencil, fp64 tables and outer state",
+            "precond": "g1",
+            "precision": f"fp32 rows/FFT, cross-quadrant inverse {STENCIL_NAMES[args.stencil]}, fp64 tables and "
+                         "outer state",
             "parallelism": f"replicas x{world}", "l2": "inputs (268 MB/step) larger than L2; no flush"}
 
 
@@ -292,7 +300,8 @@ def run_ours(args):
     C = pkg._lib
     n, N, B = args.n, 1 << args.n, args.batch
 
-    H = pkg.FastHybridGpu(n, deg_cap=P_CAP, dense_cap=DENSE_CAP, precision="fp32", device=dev)
+    H = pkg.FastHybridGpu(n, deg_cap=P_CAP, dense_cap=DENSE_CAP, precision="fp32", device=dev,
+                          stencil_precision=args.stencil)
     b_dev = sinograms(pkg, n, B, seed0=1000 * rank, device=dev)
     pipe = H.pipeline(B)
 

@@ -158,10 +158,12 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
  * y, x, x_prev, x_new are FP64; s and the stencil iterates are dtype (F32, F64 or F32X2, float-float on the FP32
  * pipe). One thread-block cluster per image keeps the
  * image in shared memory for every stencil step. g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
- * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). Supported: n <= adrt_outer_step_max_n(dtype). */
+ * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). om_img (nullable, DEVICE, with x given): per-image pairs
+ * (om_a, om_1) that replace om_a and om_1, so that images at different outer iterations step together (slot-level
+ * serving). Supported: n <= adrt_outer_step_max_n(dtype). */
 int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                     const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
-                    double a0, int precond, int g1_deg, const double* g1_coef, void* stream);
+                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, void* stream);
 int adrt_outer_step_max_n(int dtype);
 
 /* Dense low-frequency rows (fastops.py:28-40, 100-117): for r < nrows and every image b,

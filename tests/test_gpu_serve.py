@@ -41,11 +41,12 @@ def test_graph_replay_matches_eager(pkg, golden):
     assert pipe.device_bytes() == Pipeline.estimate_bytes(inv.plan, 3, "fp32")
 
 
-def _serve(pkg, golden, budget, seed):
+def _serve(pkg, golden, budget, seed, lane="slot"):
     from adrt_pinv_gb300 import serve
 
     invs = _inverses(pkg, golden)
-    S = serve.InverseServer(lambda n: invs[n], slots=lambda n: 4, hbm_budget_bytes=budget)
+    cls = serve.SlotLane if lane == "slot" else serve.Lane
+    S = serve.InverseServer(lambda n: invs[n], slots=lambda n: 4, hbm_budget_bytes=budget, lane_cls=cls)
     rng = np.random.default_rng(seed)
     sizes = rng.choice([4, 5, 6], size=30)
     sinos = {n: _sinos(pkg, n, int((sizes == n).sum()), 100 * n) for n in (4, 5, 6)}
@@ -63,19 +64,32 @@ def _serve(pkg, golden, budget, seed):
     return S, invs
 
 
-def test_served_mix_equals_alone(pkg, golden):
-    S, _ = _serve(pkg, golden, 120e9, 0)
-    assert S.max_busy >= 2  # batches of different sizes were in flight together
+@pytest.mark.parametrize("lane", ["slot", "batch"])
+def test_served_mix_equals_alone(pkg, golden, lane):
+    S, _ = _serve(pkg, golden, 120e9, 0, lane)
+    assert S.max_busy >= 2  # lanes of different sizes were in flight together
     assert S.evictions == 0
+    if lane == "slot":  # requests of one size overlapped on the device at different outer iterations
+        assert any(l.steps_run < sum(1 for r in S.finished if r.n == n) * l.D for n, l in S.lanes.items())
 
 
-def test_served_mix_under_small_budget(pkg, golden):
+@pytest.mark.parametrize("lane", ["slot", "batch"])
+def test_served_mix_under_small_budget(pkg, golden, lane):
     from adrt_pinv_gb300 import serve
 
     invs = _inverses(pkg, golden)
-    big = max(serve.Lane.estimate_bytes(invs[n], 4) for n in invs)
-    S, _ = _serve(pkg, golden, big + 1, 1)
+    cls = serve.SlotLane if lane == "slot" else serve.Lane
+    big = max(cls.estimate_bytes(invs[n], 4) for n in invs)
+    S, _ = _serve(pkg, golden, big + 1, 1, lane)
     assert S.evictions >= 1 and S.memory_in_use() <= big + 1
+
+
+def test_slot_lane_device_bytes_match_estimate(pkg, golden):
+    from adrt_pinv_gb300 import serve
+
+    inv = _inverses(pkg, golden)[6]
+    lane = serve.SlotLane(inv, 4, "cuda")
+    assert lane.device_bytes() <= serve.SlotLane.estimate_bytes(inv, 4)
 
 
 def test_public_apply_graph_replay(pkg, golden):

@@ -40,15 +40,69 @@ class FakeLane:
     def release(self):
         self.released = True
 
+    # the server's lane interface (batch-level)
+    def free_slots(self):
+        return self.slots if self.batch is None else 0
 
-def _server(pkg, budget, slots=lambda n: 4):
+    def admit(self, reqs):
+        self.launch(reqs)
+
+    def poll(self, keep=None):
+        return self.collect(keep) if self.done() else []
+
+    def advance(self):
+        pass
+
+    def in_flight(self):
+        return len(self.batch) if self.batch else 0
+
+
+class FakeSlotLane(FakeLane):
+    """Slot-level: each admitted request finishes D advance() calls later; free slots take new requests at once."""
+
+    D = 3
+
+    def __init__(self, inv, slots, device):
+        super().__init__(inv, slots, device)
+        self.req = [None] * slots
+        self.k = [0] * slots
+        self.out = []
+        self.steps = 0
+
+    def free_slots(self):
+        return sum(r is None for r in self.req)
+
+    def admit(self, reqs):
+        free = [i for i, r in enumerate(self.req) if r is None]
+        assert len(reqs) <= len(free)
+        for i, r in zip(free, reqs):
+            self.req[i], self.k[i] = r, 0
+
+    def advance(self):
+        if not any(self.req):
+            return
+        self.steps += 1
+        for i, r in enumerate(self.req):
+            if r is not None:
+                self.k[i] += 1
+                if self.k[i] == self.D:
+                    r.result = ("x", r.rid, self.inv.n)
+                    self.out.append(r)
+                    self.req[i] = None
+
+    def poll(self, keep=None):
+        out, self.out = self.out, []
+        return out
+
+    def in_flight(self):
+        return sum(r is not None for r in self.req) + len(self.out)
+
+
+def _server(pkg, budget, slots=lambda n: 4, lane=FakeLane):
     from adrt_pinv_gb300 import serve
 
-    class S(serve.InverseServer):
-        lane_cls = FakeLane
-
     FakeLane.created = []
-    return S(FakeInverse, slots, hbm_budget_bytes=budget, device="cpu"), serve
+    return serve.InverseServer(FakeInverse, slots, hbm_budget_bytes=budget, device="cpu", lane_cls=lane), serve
 
 
 def test_batches_and_results(pkg):
@@ -111,3 +165,26 @@ def test_pipeline_estimate_matches_buffers(pkg):
     expect += 2 * nd * N * N * 8 + nd * B * N * 8 + L * 8 + 3 * L * 4 + plan.coef.size * 4
     assert est == expect
     assert Pipeline.estimate_bytes(plan, 3, "fp32") - est == B * 4 * (2 * N - 1) * N * 8
+
+
+def test_slot_level_admission_between_steps(pkg):
+    """A request that arrives while a slot lane is busy starts at the next step in a free slot, without waiting for
+    the requests ahead of it to finish."""
+    S, serve = _server(pkg, budget=1e12, slots=lambda n: 2, lane=FakeSlotLane)
+    a, b, c = (serve.Request(i, 5, None) for i in range(3))
+    S.submit(a)
+    S.step()  # a admitted and one step run
+    lane = S.lanes[5]
+    assert lane.req[0] is a and lane.k[0] == 1
+    S.submit(b)
+    S.submit(c)
+    S.step()  # b takes the free slot while a is mid-way; c waits for a slot
+    assert lane.req[1] is b and lane.k == [2, 1] and len(S.queues[5]) == 1
+    S.step()  # a finishes (k = 3); its slot frees
+    assert a.result == ("x", 0, 5) and lane.req[0] is None
+    S.step()  # a collected, c admitted into slot 0 and stepped together with b's last step
+    assert lane.req[0] is c and lane.k[0] == 1 and b.result == ("x", 1, 5)
+    while S.step():
+        pass
+    assert {r.rid for r in S.finished} == {0, 1, 2}
+    assert lane.steps == 6  # a: steps 1-3, b: 2-4, c: 4-6, overlapping
