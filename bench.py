@@ -67,7 +67,8 @@ def config(args, world):
                         f"10-ellipse phantoms + noise {REL_SIGMA:g} max|b|",
             "N": N, "global_batch": args.batch * world, "p": P_CAP, "dense_cap": DENSE_CAP, "method": "hybrid",
             "precond": "g1",
-            "precision": f"fp32 rows/FFT, cross-quadrant inverse {STENCIL_NAMES[args.stencil]}, fp64 tables and "
+            "precision": f"fp32 rows/FFT, cross-quadrant inverse {STENCIL_NAMES[getattr(args, 'stencil', STENCIL)]}, "
+                         "fp64 tables and "
                          "outer state",
             "parallelism": f"replicas x{world}", "l2": "inputs (268 MB/step) larger than L2; no flush"}
 
