@@ -74,6 +74,7 @@ PROTOTYPES = {
     "adrt_launch_count": [],
     "adrt_fp32_probe": [_I, _I, _I, _P, _P],
     "adrt_rows_run": [ctypes.POINTER(RowJob), _P],
+    "adrt_rows_ff_run": [ctypes.POINTER(RowJob), _P],
     "adrt_twiddle_table": [_I, _I, _I, _P, _P, _P],
     "adrt_power_rows": [_I, _I, _I, _P, _P, _I, _I, _D, _P, _P, _P],
     "adrt_cert_rowsum_dev": [_I, _I, _P, _I, _P, _P],

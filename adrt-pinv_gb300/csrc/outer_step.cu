@@ -10,49 +10,14 @@
 #include <cooperative_groups.h>
 
 #include "common.cuh"
+#include "ff.cuh"
 #include "launch.h"
 
 namespace cg = cooperative_groups;
 
 namespace adrt {
 
-// ------------------------------------------------------------------ stencil arithmetic: FP32, FP64 or float-float
-// Float-float ("double-float") numbers: an unevaluated sum hi + lo of two FP32 values with |lo| <= ulp(hi)/2, about
-// 48 significant bits, on the FP32 pipe (GB300's FP64 rate is a small fraction of its FP32 rate). Error-free
-// transformations: TwoSum (Knuth, 6 operations, any magnitudes), Fast2Sum (Dekker, |a| >= |b|) and TwoProd through
-// one fused multiply-add; double-word sum and product as in Joldes, Muller and Popescu, "Tight and rigorous error
-// bounds for basic building blocks of double-word arithmetic", ACM TOMS 44 (2017): DWPlusDW (Algorithm 6, relative
-// error below 3u^2) and DWTimesDW (Algorithm 12, below 4u^2), u = 2^-24. Every operation is an explicitly rounded
-// intrinsic, so the compiler neither contracts nor reassociates them.
-struct ff {
-    float hi, lo;
-};
-
-__device__ __forceinline__ ff two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    const float ap = __fsub_rn(s, b);
-    const float bp = __fsub_rn(s, ap);
-    return {s, __fadd_rn(__fsub_rn(a, ap), __fsub_rn(b, bp))};
-}
-__device__ __forceinline__ ff fast_two_sum(float a, float b) {
-    const float s = __fadd_rn(a, b);
-    return {s, __fsub_rn(b, __fsub_rn(s, a))};
-}
-__device__ __forceinline__ ff ff_add(ff x, ff y) {
-    const ff s = two_sum(x.hi, y.hi);
-    const ff t = two_sum(x.lo, y.lo);
-    const ff v = fast_two_sum(s.hi, __fadd_rn(s.lo, t.hi));
-    return fast_two_sum(v.hi, __fadd_rn(t.lo, v.lo));
-}
-__device__ __forceinline__ ff ff_neg(ff x) { return {-x.hi, -x.lo}; }
-__device__ __forceinline__ ff ff_mul(ff x, ff y) {
-    const float ch = __fmul_rn(x.hi, y.hi);
-    const float cl1 = __fmaf_rn(x.hi, y.hi, -ch);
-    const float tl1 = __fmaf_rn(x.hi, y.lo, __fmul_rn(x.lo, y.lo));
-    const float cl2 = __fmaf_rn(x.lo, y.hi, tl1);
-    return fast_two_sum(ch, __fadd_rn(cl1, cl2));
-}
-
+// ------------------------------------------------------------------ stencil arithmetic: FP32, FP64 or float-float (ff.cuh)
 // arithmetic of one stencil element type: add, sub, mul, exact scaling by powers of two, conversions from/to FP64
 template <typename T> struct StencilArith {
     using V = T;

@@ -67,6 +67,15 @@ class RowTables:
         self.row_grid = 0  # CTAs of the row programs (0: one per SM); set by the autotuner
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self._zd = None
+        # compensated high rows: float-float kernel in an FP32 pipeline; an FP64 pipeline runs them as ordinary
+        # polynomial rows (FP64 is accurate enough there)
+        self.high_poly = getattr(plan, "high_rows", "dense") == "ff" and len(plan.dense_freqs) > 0
+        self.high_ff = self.high_poly and real == torch.float32
+        if self.high_ff:
+            # the compensated rows read the roots of unity and the filter constants in FP64
+            self.roots64 = torch.from_numpy(roots_of_unity(plan.L)).to(device=device, dtype=torch.complex128)
+            self.coef64 = torch.from_numpy(np.ascontiguousarray(plan.coef.ravel())).to(device=device,
+                                                                                      dtype=torch.float64)
 
     def job(self, Y, ops, rows):
         p = self.plan
@@ -165,10 +174,18 @@ class RowTables:
         C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(T), C.ptr(Y), R * N,
                C.ptr(self._zd), C.ptr(self.err), mode, C.stream_handle())
 
+    def run_ff(self, Y, ops):
+        """The op list on the high-condition rows in float-float arithmetic (adrt_rows_ff_run)."""
+        j = self.job(Y, ops, self.rows_dense)
+        j.roots = self.roots64.data_ptr()
+        j.coef = self.coef64.data_ptr()
+        C.call("adrt_rows_ff_run", ctypes.byref(j), C.stream_handle())
+
     def run(self, Y, ops):
         """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take the exact
         filter (fastops.py:100-117), fused with the butterflies around it (adjoint levels before, Gram levels and
-        the level-1 butterflies of the hybrid around it) into one precomputed operator per row."""
+        the level-1 butterflies of the hybrid around it) into one precomputed operator per row; with compensated
+        high rows (plan.high_rows == "ff") they keep the polynomial filter in float-float arithmetic instead."""
         ops = fuse_ops(ops)
         B = Y.shape[0]
         if not ops:
@@ -178,6 +195,15 @@ class RowTables:
         if len(pidx) > 1:
             raise ValueError("at most one filter op per list")
         dense = len(self.plan.dense_freqs) > 0
+        if dense and self.high_poly:
+            if self.high_ff:
+                self._timed_main(Y, ops, st)
+                self.run_ff(Y, ops)
+            else:
+                rows = torch.cat([self.rows_main, self.rows_dense])
+                C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, rows)), st)
+            self.count += B * self.plan.level_rows(ops_unfused(ops))
+            return
         if not dense or not pidx:
             if dense:
                 rows = torch.cat([self.rows_main, self.rows_dense])
@@ -437,6 +463,8 @@ class Pipeline:
         t = self.tables
         bufs = [self.Y, self.parts, self.y, self.s, *self.xs, *self.st, t.roots, t.deg, t.coef, t.rows_main,
                 t.rows_dense, *t._dense_dev.values()]
+        if t.high_ff:
+            bufs += [t.roots64, t.coef64]
         if t._zd is not None:
             bufs.append(t._zd)
         if getattr(self, "b_in", None) is not None:
@@ -452,9 +480,13 @@ class Pipeline:
         rs = PRECISIONS[precision].itemsize
         ss = STENCIL_PRECISIONS[stencil_precision or precision].itemsize
         nd = 2 * len(plan.dense_freqs)
+        ff = getattr(plan, "high_rows", "dense") == "ff" and nd > 0
         img = B * N * N
         total = B * 2 * L * N * 2 * rs + 3 * img * rs + 4 * img * 8 + 4 * img * ss
-        total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
+        if ff:  # FP64 roots and coefficients of the compensated rows instead of dense operators
+            total += L * 16 + plan.coef.size * 8
+        else:
+            total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
         total += L * 2 * rs + 3 * L * 4 + plan.coef.size * rs  # roots; deg and the row lists; coefficients
         if captured:
             total += B * 4 * (2 * N - 1) * N * 8

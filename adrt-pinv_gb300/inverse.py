@@ -8,7 +8,9 @@ run everything on one GPU:
     Lanczos (scipy eigsh, as the reference) whose matvecs are the device operator in FP64;
   * apply: the device pipeline (pack+FFT, fused row engine, iFFT+unpack, G_1 stencil, outer update).
 Extra keywords: deg_cap (degree-p filter: d_k <- min(p, d_k)), precision ('fp32' | 'fp64'), outer=(lo, hi, D) to
-inject a precomputed outer interval, device.
+inject a precomputed outer interval, device, high_rows ('dense': the rows with d_k > dense_cap take the exact dense
+filter, as the reference; 'ff': they keep the polynomial filter in float-float arithmetic, compensated rows without
+operator memory), stencil_precision (hybrid: 'fp32' | 'ff' | 'fp64' for the cross-quadrant preconditioner).
 
 `apply` accepts one sinogram (4, 2N-1, N) or a batch (B, 4, 2N-1, N), as NumPy (host) or torch (CUDA) arrays, and
 returns the same kind: NumPy FP64 for NumPy input, a torch FP64 CUDA tensor for CUDA input.
@@ -76,7 +78,7 @@ class _GpuInverse:
     m_lo = 1
 
     def _setup(self, n, tau_fac, eps_in, eps, threads, lam_max, power_iters, safety, dense_cap, deg_cap, precision,
-               outer, device, lam_bound, precond="none", g1_deg=14, stencil_precision=None):
+               outer, device, lam_bound, precond="none", g1_deg=14, stencil_precision=None, high_rows="dense"):
         if not torch.cuda.is_available():
             raise RuntimeError("a CUDA device is required (no CPU fallback)")
         C.load()
@@ -100,8 +102,10 @@ class _GpuInverse:
                 lam_max = explicit_lam_max(n, self.oms)
             else:
                 raise ValueError(f"lam_bound {lam_bound!r}")
+        if high_rows == "ff" and precision != "fp32":
+            high_rows = "dense"  # in FP64 the polynomial rows are exact enough; the compensated kernel is FP32-only
         self.plan = Plan(self.method, n, lam_max, tau_fac, eps_in, eps, deg_cap=deg_cap, dense_cap=dense_cap,
-                         precond=precond, g1_deg=g1_deg)
+                         precond=precond, g1_deg=g1_deg, high_rows=high_rows)
         self.lam_max, self.deg = self.plan.lam_max, self.plan.deg
         self.eng = EngineInfo(len(self.plan.dense_freqs))
         self._pipes = {}
@@ -240,9 +244,10 @@ class FastLpGpu(_GpuInverse):
     m_lo = 1
 
     def __init__(self, n, tau_fac=0.2, eps_in=0.1, eps=1e-10, threads=8, lam_max=None, power_iters=40, safety=1.5,
-                 dense_cap=None, lam_bound="power", deg_cap=None, precision="fp32", outer=None, device="cuda"):
+                 dense_cap=None, lam_bound="power", deg_cap=None, precision="fp32", outer=None, device="cuda",
+                 high_rows="dense"):
         self._setup(n, tau_fac, eps_in, eps, threads, lam_max, power_iters, safety, dense_cap, deg_cap, precision, outer,
-                    device, lam_bound)
+                    device, lam_bound, high_rows=high_rows)
 
     def frame_window(self, x):
         """E^T sum_q T_q^T [M p(M)] T_q E x (fastops.py:277-281), FP64 N x N in and out."""
@@ -259,12 +264,12 @@ class FastHybridGpu(_GpuInverse):
 
     def __init__(self, n, tau_fac=0.2, eps_in=0.1, eps=1e-10, threads=8, lam_max=None, g1_deg=14, power_iters=40,
                  safety=1.5, dense_cap=None, precond="g1", lam_bound="power", deg_cap=None, precision="fp32", outer=None,
-                 device="cuda", stencil_precision=None):
+                 device="cuda", stencil_precision=None, high_rows="dense"):
         if n < 2:
             raise ValueError("the hybrid inverse needs n >= 2")
         self.g1_deg, self.precond = g1_deg, precond
         self._setup(n, tau_fac, eps_in, eps, threads, lam_max, power_iters, safety, dense_cap, deg_cap, precision, outer,
-                    device, lam_bound, precond, g1_deg, stencil_precision)
+                    device, lam_bound, precond, g1_deg, stencil_precision, high_rows)
 
     def Gh(self, x):
         """G_h x (fastops.py:325-331), FP64 N x N in and out."""

@@ -86,7 +86,7 @@ class Plan:
     dense_cap: rows with d_k > dense_cap use the exact Tikhonov filter (fastops.py:28-40); outer = (lo, hi, D)."""
 
     def __init__(self, method, n, lam_max, tau_fac=0.2, eps_in=0.1, eps=1e-10, deg=None, deg_cap=None, dense_cap=None,
-                 precond="g1", g1_deg=14, outer=None, raw_lam=False):
+                 precond="g1", g1_deg=14, outer=None, raw_lam=False, high_rows="dense"):
         if method not in METHODS:
             raise ValueError(f"method must be one of {METHODS}")
         if not (1 <= n <= 11):
@@ -113,6 +113,12 @@ class Plan:
         self.deg = d
         self.deg_cap, self.dense_cap = deg_cap, dense_cap
         self.dense_freqs = np.nonzero(d > dense_cap)[0].astype(np.int64) if dense_cap is not None else np.zeros(0, np.int64)
+        # the rows with d_k > dense_cap: "dense" applies the reference's exact dense filter (fastops.py:28-40, the
+        # operators held on the device), "ff" keeps the polynomial filter and runs those rows' op lists in
+        # float-float arithmetic (compensated rows: no operator memory, more arithmetic)
+        if high_rows not in ("dense", "ff"):
+            raise ValueError("high_rows must be 'dense' or 'ff'")
+        self.high_rows = high_rows
         self.dense_tables = None
         self.coef, self.coef_stride = coef_table(self.lam_max, self.tau, self.deg)
         self.set_outer(outer)
@@ -138,14 +144,15 @@ class Plan:
     def level_rows(self, ops, dense_rows=None):
         """Level-row count of one packed op list, as the reference counts it (fastops.py:144-153, 117)."""
         R, n = 2 * self.L, self.n
-        nd = 2 * len(self.dense_freqs)
+        poly_high = getattr(self, "high_rows", "dense") == "ff"  # compensated rows keep the polynomial filter
+        nd = 0 if poly_high else 2 * len(self.dense_freqs)
         tot = 0
         for op, lo, hi in ops:
             if op in ("B", "BT"):
                 tot += R * (hi - lo + 1)
             elif op == "P":
                 d = np.tile(self.deg, 2)
-                keep = ~np.isin(np.arange(R) % self.L, self.dense_freqs)
+                keep = np.ones(R, bool) if poly_high else ~np.isin(np.arange(R) % self.L, self.dense_freqs)
                 tot += int(np.sum(np.maximum(d[keep] - 1, 0))) * 2 * (hi - lo + 1)
                 tot += nd * self.N // max(1, n)
         return tot

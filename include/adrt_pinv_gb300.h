@@ -107,6 +107,12 @@ typedef struct adrt_row_job {
 
 int adrt_rows_run(const adrt_row_job* job, void* stream);
 
+/* The same op lists on FP32 rows (dtype ADRT_F32) in float-float arithmetic (compensated rows, about 48 significant
+ * bits on the FP32 pipe), for the high-condition low-frequency rows where the FP32 filter loses accuracy
+ * (cpp/oblique.cpp:74-104 evaluated in extended precision). Here `roots` (mode 0 only) holds the L roots of unity in
+ * FP64 (complex128) and `coef` the filter table in FP64; rows are read and written in FP32. */
+int adrt_rows_ff_run(const adrt_row_job* job, void* stream);
+
 /* Per-row twiddle table tab[k*(N/2+1) + t] = z_k^t (t = 0..N/2) from K complex z (FP64 in, dtype out),
  * by binary powering in FP64. */
 int adrt_twiddle_table(int dtype, int n, int K, const double* z, void* tab, void* stream);

@@ -218,3 +218,45 @@ def test_fused_cross_quadrant_inverse_high_precision(pkg, sprec, tol, n, nimg):
     got = out.cpu().numpy()
     for i in range(min(nimg, 3)):
         assert rel_err(got[i], O.g1_inv(s[i])) < tol
+
+
+@pytest.mark.parametrize("cap", [16, 8])
+def test_n256_compensated_rows_without_dense_operators(pkg, cap):
+    """The rows with d_k > cap keep the polynomial filter, evaluated in float-float (compensated) arithmetic, and
+    no dense operator is stored: the FP32 inverse against the reference's C++-engine path on the same plan (every
+    row polynomial, FP64) stays within 1e-5, where the plain FP32 polynomial rows give about 3e-5."""
+    H = pkg.FastHybridGpu(8, deg_cap=32, dense_cap=cap, precision="fp32", high_rows="ff")
+    n, N = 8, 256
+    assert H.eng.n_dense > 0 and H.pipeline(1).tables.high_ff
+    x = pkg.phantoms.ellipse_phantom(N, seed=7)
+    b = pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, x), 1e-3, seed=8)
+    ref = CE.hybrid_cpu(n, dict(lam_max=H.lam_max, deg=H.deg, outer=(H.lo, H.hi, H.outer_deg)), threads=16).apply(b)
+    got = H.apply(b)
+    assert not H.pipeline(1).tables._dense_dev  # no operator was built
+    assert rel_err(got, ref) < 1e-5
+
+
+@pytest.mark.parametrize("method", ["lp", "hybrid"])
+def test_compensated_rows_match_fp64_rows(pkg, method):
+    """Row level: both op lists of each method on the high rows in float-float equal the FP64 row engine to about
+    FP32 output rounding (2e-7), well below the FP32 polynomial rows' error on the same rows."""
+    import torch
+
+    from adrt_pinv_gb300.device import RowTables, _op_lists
+
+    n, N = 6, 64
+    cls = pkg.FastLpGpu if method == "lp" else pkg.FastHybridGpu
+    H = cls(n, deg_cap=32, dense_cap=8, precision="fp32", high_rows="ff")
+    plan = H.plan
+    t32 = RowTables(plan, torch.float32, torch.device("cuda"))
+    t64 = RowTables(plan, torch.float64, torch.device("cuda"))
+    rows = t32.rows_dense.long()
+    g = torch.Generator(device="cuda").manual_seed(1)
+    Y = torch.randn((2, 4 * N, N), dtype=torch.complex128, device="cuda", generator=g)
+    for ops in _op_lists(plan).values():
+        ref = Y.clone()
+        t64.run(ref, ops)
+        got = Y.to(torch.complex64)
+        t32.run(got, ops)
+        err = ((got.to(torch.complex128) - ref)[:, rows].abs().max() / ref[:, rows].abs().max()).item()
+        assert err < 2e-6, (ops, err)
