@@ -83,7 +83,7 @@ PROTOTYPES = {
     "adrt_resid": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P],
     "adrt_g1_step": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _P],
     "adrt_lorr": [_I, _I, _I, _P, _P, _P],
-    "adrt_outer_update": [_I, _I, _I, _P, _P, _P, _I, _P, _D, _D, _D, _P],
+    "adrt_outer_update": [_I, _I, _I, _P, _P, _P, _I, _P, _D, _D, _D, _P, _P],
     "adrt_sum3": [_I, _I, _I, _P, _P, _P, _P, _I, _P],
     "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _P],
     "adrt_outer_step_max_n": [_I],

@@ -262,8 +262,8 @@ int adrt_lorr(int dtype, int n, int nimg, const void* s, void* out, void* stream
 }
 
 int adrt_outer_update(int dtype, int n, int nimg, const void* x, const void* x_prev, const void* r, int rdtype,
-                      void* x_new, double om_a, double om_1, double a0, void* stream) {
-    return image_outer(dtype, n, nimg, x, x_prev, r, rdtype, x_new, om_a, om_1, a0, as_stream(stream));
+                      void* x_new, double om_a, double om_1, double a0, const double* om_img, void* stream) {
+    return image_outer(dtype, n, nimg, x, x_prev, r, rdtype, x_new, om_a, om_1, a0, om_img, as_stream(stream));
 }
 
 int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const void* p2, void* out, int out_dtype,

@@ -83,9 +83,10 @@ __global__ void lorr_kernel(int n, size_t total, const T* __restrict__ s, T* __r
 }
 
 // x_new = x + om_a r + om_1 (x - x_prev); x == NULL: x_new = a0 r (fastops.py:251-257). r may be narrower than x.
+// om_img (nullable): per-image (om_a, om_1) pairs, images of `per` elements
 template <typename T, typename TR>
 __global__ void outer_kernel(size_t total, const T* __restrict__ x, const T* __restrict__ xp, const TR* __restrict__ r,
-                             T* __restrict__ xn, T om_a, T om_1, T a0) {
+                             T* __restrict__ xn, T om_a, T om_1, T a0, const double* __restrict__ om_img, size_t per) {
     for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
         const T rv = (T)r[e];
         if (!x) {
@@ -93,7 +94,13 @@ __global__ void outer_kernel(size_t total, const T* __restrict__ x, const T* __r
         } else {
             const T xv = x[e];
             const T prev = xp ? xp[e] : (T)0;
-            xn[e] = xv + om_a * rv + om_1 * (xv - prev);
+            T oa = om_a, o1 = om_1;
+            if (om_img) {
+                const size_t img = e / per;
+                oa = (T)om_img[2 * img];
+                o1 = (T)om_img[2 * img + 1];
+            }
+            xn[e] = xv + oa * rv + o1 * (xv - prev);
         }
     }
 }
@@ -171,7 +178,7 @@ int image_lorr(int dtype, int n, int nimg, const void* s, void* out, cudaStream_
 }
 
 int image_outer(int dtype, int n, int nimg, const void* x, const void* xp, const void* r, int rdtype, void* xn,
-                double om_a, double om_1, double a0, cudaStream_t st) {
+                double om_a, double om_1, double a0, const double* om_img, cudaStream_t st) {
     if (!img_args_ok(dtype, n, nimg, "outer_update") || (rdtype != ADRT_F32 && rdtype != ADRT_F64) ||
         (dtype == ADRT_F32 && rdtype == ADRT_F64)) {
         set_error("outer_update: bad dtypes (%d, r %d)", dtype, rdtype);
@@ -179,17 +186,18 @@ int image_outer(int dtype, int n, int nimg, const void* x, const void* xp, const
     }
     const size_t total = (size_t)nimg << (2 * n);
     if (!total) return ADRT_OK;
-    if (!r || !xn) { set_error("outer_update: null pointer"); return ADRT_EINVAL; }
+    if (!r || !xn || (om_img && !x)) { set_error("outer_update: null pointer"); return ADRT_EINVAL; }
     const int g = grid_for(total);
+    const size_t per = (size_t)1 << (2 * n);
     if (dtype == ADRT_F32)
         outer_kernel<float, float><<<g, 256, 0, st>>>(total, (const float*)x, (const float*)xp, (const float*)r, (float*)xn,
-                                                      (float)om_a, (float)om_1, (float)a0);
+                                                      (float)om_a, (float)om_1, (float)a0, om_img, per);
     else if (rdtype == ADRT_F64)
         outer_kernel<double, double><<<g, 256, 0, st>>>(total, (const double*)x, (const double*)xp, (const double*)r,
-                                                        (double*)xn, om_a, om_1, a0);
+                                                        (double*)xn, om_a, om_1, a0, om_img, per);
     else
         outer_kernel<double, float><<<g, 256, 0, st>>>(total, (const double*)x, (const double*)xp, (const float*)r,
-                                                       (double*)xn, om_a, om_1, a0);
+                                                       (double*)xn, om_a, om_1, a0, om_img, per);
     return launch_status("outer_kernel");
 }
 

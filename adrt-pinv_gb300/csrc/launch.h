@@ -20,7 +20,7 @@ int image_g1_step(int dtype, int n, int nimg, const void* s, const void* x, cons
                   double om_1, double a0, cudaStream_t st);
 int image_lorr(int dtype, int n, int nimg, const void* s, void* out, cudaStream_t st);
 int image_outer(int dtype, int n, int nimg, const void* x, const void* xp, const void* r, int rdtype, void* xn,
-                double om_a, double om_1, double a0, cudaStream_t st);
+                double om_a, double om_1, double a0, const double* om_img, cudaStream_t st);
 // set the dynamic shared-memory limit of a kernel once per size (safe to call before and during stream capture)
 int ensure_smem(const void* func, size_t bytes);
 // spatial ADRT levels; active (nullable): images with active[img] == 0 are skipped

@@ -444,9 +444,21 @@ class Pipeline:
                C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
                p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), C.stream_handle())
 
-    def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0):
+    def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0, om_img=None):
+        """x_new = x + om_a r + om_1 (x - x_prev) (x None: a0 r); om_img (device (B, 2) FP64, optional): per-image
+        (om_a, om_1)."""
         C.call("adrt_outer_update", C.dtype_code(x_new.dtype), self.plan.n, self.B, C.ptr(x), C.ptr(x_prev), C.ptr(r),
-               C.dtype_code(r.dtype), C.ptr(x_new), om_a, om_1, a0, C.stream_handle())
+               C.dtype_code(r.dtype), C.ptr(x_new), om_a, om_1, a0, C.ptr(om_img), C.stream_handle())
+
+    def step_all(self, y, x, x_prev, x_new, om_img):
+        """One outer step of every image with per-image coefficients (x_new = x + om_a P(y - G x) + om_1 (x - x_prev)
+        with G x already in the partial images): the fused kernel where it exists, else the separate kernels."""
+        if self.fused_outer_ok():
+            self.fused_outer_step(y, True, x, x_prev, x_new, 0.0, 0.0, 0.0, om_img=om_img)
+            return
+        s = self.resid(y)
+        r = self.precond(s) if self.plan.method == "hybrid" else s
+        self.outer_step(x, x_prev, r, x_new, 0.0, 0.0, 0.0, om_img=om_img)
 
     # ---------------------------------------------------------------- operators
     def G(self, x):

@@ -194,7 +194,7 @@ class SlotLane:
         cur, prev, new = self._bufs(ph)
         torch.index_select(self.coef_tab, 0, self.k, out=self.om)
         self.pipe.G(cur)
-        self.pipe.fused_outer_step(self.pipe.y, True, cur, prev, new, 0.0, 0.0, 0.0, om_img=self.om)
+        self.pipe.step_all(self.pipe.y, cur, prev, new, self.om)
         self.k.add_(1).clamp_(max=self.D)
 
     # the server's lane interface

@@ -153,7 +153,7 @@ int adrt_g1_step(int dtype, int n, int nimg, const void* s, const void* x, const
                  double om_1, double a0, void* stream);
 int adrt_lorr(int dtype, int n, int nimg, const void* s, void* out, void* stream);
 int adrt_outer_update(int dtype, int n, int nimg, const void* x, const void* x_prev, const void* r, int rdtype,
-                      void* x_new, double om_a, double om_1, double a0, void* stream);
+                      void* x_new, double om_a, double om_1, double a0, const double* om_img, void* stream);
 int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const void* p2, void* out, int out_dtype,
               void* stream);
 

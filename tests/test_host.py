@@ -75,7 +75,9 @@ def test_argument_validation_without_gpu(lib):
     assert lib.adrt_pack_fft(0, 12, 1, 0, 0, None, None, None, None) == 1
     assert lib.adrt_ifft_unpack(0, 3, 1, None, None, None, None, None, None) == 1
     assert lib.adrt_forward(0, 0, 1, None, None, None, None) == 1
-    assert lib.adrt_outer_update(0, 3, 1, None, None, None, 1, None, 0.0, 0.0, 0.0, None) == 1  # f64 r into f32 x
+    assert lib.adrt_outer_update(0, 3, 1, None, None, None, 1, None, 0.0, 0.0, 0.0, None, None) == 1  # f64 r, f32 x
+    assert lib.adrt_rows_ff_run(None, None) == 1
+    assert lib.adrt_cgls_start(None, None, None) == 1 and lib.adrt_pcg_step(None, None) == 1
 
 
 @pytest.mark.parametrize("method,n", [("lp", 4), ("hybrid", 6), ("hybrid", 4), ("lp", 6)])
