@@ -391,7 +391,10 @@ def run_ours(args):
                             "achieved": achieved, "peak": peak / 1e12, "unit": "TFLOP/s", "frac": achieved * 1e12 / peak,
                             "peak_source": "measured in this run: FP32 FMA probe kernel",
                             "flop_per_launch": flops_per_launch, "launch_ms": rows_launch_ms,
-                            "traffic": tr, "traffic_unit": "bytes/launch (ncu dram read+write)"}
+                            "traffic": tr, "traffic_unit": "bytes/launch (ncu dram read+write)",
+                            "traffic_source": ("not measured in this run: the committed ncu capture "
+                                               "profiles/rows_prog_kernel_hybrid_n8_b64_dram.txt (N=256, batch 64), "
+                                               "scaled by batch/64" if tr is not None else None)}
     if not args.no_cpu_baseline:
         plan_kw = dict(lam_max=H.plan.lam_max, deg=H.deg, dense_cap=DENSE_CAP, outer=(H.lo, H.hi, H.outer_deg))
         b_one = b_dev[0].cpu().numpy()
@@ -409,10 +412,60 @@ def run_ours(args):
     if world == 1 and not args.no_extras:
         other = "ff" if args.stencil != "ff" else "fp32"
         line[f"preconditioner_{other}"] = stencil_variant(pkg, H, b_dev, args.steps, other, ref, torch)
+        line["adrt_int32"] = adrt_int32_timing(pkg, n, B, args.steps, torch)
         line.update(extras(pkg, dev, args))
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
+
+
+def adrt_int32_timing(pkg, n, B, steps, torch):
+    """The spatial ADRT forward and transpose on B int32 images with values in [0, 255] (bit-exact integer sums),
+    each timed with CUDA events; HBM roofline per call from the bytes every level pass moves (level m reads the
+    level-(m-1) data and writes level m; the transpose mirrors it; the first forward level reads the image, the last
+    transpose level writes it), against the measured copy bandwidth; checked bit-exact against the oracle on one
+    image."""
+    from oracle import adrt_np as A
+
+    N = 1 << n
+    dev = torch.device("cuda")
+    g = torch.Generator(device=dev).manual_seed(5)
+    x = torch.randint(0, 256, (B, N, N), dtype=torch.int32, device=dev, generator=g)
+    b = torch.empty((B, 4, 2 * N - 1, N), dtype=torch.int32, device=dev)
+    xt = torch.empty_like(x)
+    scratch = torch.empty(2 * B * 4 * (2 * N - 1) * N, dtype=torch.int32, device=dev)
+    C = pkg._lib
+    st = C.stream_handle()
+
+    def fwd():
+        C.call("adrt_forward", C.I32, n, B, C.ptr(x), C.ptr(b), C.ptr(scratch), st)
+
+    def adj():
+        C.call("adrt_transpose", C.I32, n, B, C.ptr(b), C.ptr(xt), C.ptr(scratch), st)
+
+    lvl = lambda m: 4 * (N + (1 << m) - 1) * N * 4  # bytes of level-m data, four quadrants, int32
+    fwd_bytes = B * (N * N * 4 + sum(lvl(m) for m in range(1, n + 1)) + sum(lvl(m) for m in range(1, n)))
+    peak, _ = measured_hbm_peak()
+    out = {}
+    for name, fn in (("forward", fwd), ("transpose", adj)):
+        for _ in range(3):
+            fn()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        gbs = fwd_bytes / (ms * 1e-3) / 1e9
+        out[name] = {"ms": ms, "images_per_s": B / (ms * 1e-3), "bytes_per_call": fwd_bytes, "achieved_gbs": gbs,
+                     "peak_gbs": peak, "frac": gbs / peak}
+    x0 = x[0].cpu().numpy()
+    out["bit_exact_forward"] = bool(np.array_equal(b[0].cpu().numpy(), A.adrt(n, x0, dtype=np.int64)))
+    out["bit_exact_transpose"] = bool(np.array_equal(xt[0].cpu().numpy(),
+                                                     A.adrt_T(n, b[0].cpu().numpy(), dtype=np.int64)))
+    out["workload"] = f"{B} int32 images N={N}, values U[0,255]"
+    return out
 
 
 def stencil_variant(pkg, H, b_dev, steps, stencil, ref, torch):
