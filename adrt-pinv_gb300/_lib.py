@@ -85,9 +85,9 @@ PROTOTYPES = {
     "adrt_lorr": [_I, _I, _I, _P, _P, _P],
     "adrt_outer_update": [_I, _I, _I, _P, _P, _P, _I, _P, _D, _D, _D, _P, _P],
     "adrt_sum3": [_I, _I, _I, _P, _P, _P, _P, _I, _P],
-    "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _P],
+    "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _I, _P],
     "adrt_outer_step_max_n": [_I],
-    "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _P],
+    "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _I, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_transpose": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_cgls_start": [ctypes.POINTER(CglsState), _P, _P],

@@ -273,16 +273,17 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
 
 int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                     const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
-                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, void* stream) {
+                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, int band,
+                    void* stream) {
     return outer_step(dtype, parts_dtype, n, nimg, y, p0, p1, p2, x, x_prev, x_new, om_a, om_1, a0, precond, g1_deg,
-                      g1_coef, om_img, as_stream(stream));
+                      g1_coef, om_img, band, as_stream(stream));
 }
 
 int adrt_outer_step_max_n(int dtype) { return outer_step_max_n(dtype); }
 
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
-                    long long img_stride, void* Zd, int32_t* err, int use_tc, void* stream) {
-    return dense_rows(dtype, n, nimg, nrows, rows, W, Y, img_stride, Zd, err, use_tc, as_stream(stream));
+                    long long img_stride, void* Zd, int32_t* err, int use_tc, int tile, void* stream) {
+    return dense_rows(dtype, n, nimg, nrows, rows, W, Y, img_stride, Zd, err, use_tc, tile, as_stream(stream));
 }
 
 int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scratch, void* stream) {

@@ -372,7 +372,11 @@ static int launch_tc(int n, int nimg, int nrows, const int* rows, const void* W,
 }
 
 int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
-               void* Zd, int* err, int use_tc, cudaStream_t st) {
+               void* Zd, int* err, int use_tc, int tile, cudaStream_t st) {
+    if (tile != 0 && tile != 16 && tile != 32 && tile != 64) {
+        set_error("dense_rows: tile must be 0 (auto), 16, 32 or 64 images per CTA");
+        return ADRT_EINVAL;
+    }
     if ((dtype != ADRT_F32 && dtype != ADRT_F64) || n < 1 || n > 11 || nimg < 0 || nrows < 0 ||
         (nimg && nrows && (!rows || !W || !Y || !Zd))) {
         set_error("dense_rows: bad arguments (dtype=%d n=%d nimg=%d nrows=%d)", dtype, n, nimg, nrows);
@@ -397,8 +401,9 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
         rc = launch_status("dense_stream_kernel");
     } else if (dtype == ADRT_F32 && use_tc && n >= 6) {
         if (!err) { set_error("dense_rows: the tensor-core path needs an error flag"); return ADRT_EINVAL; }
-        if (nimg <= 16) rc = launch_tc<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
-        else if (nimg <= 32) rc = launch_tc<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        const int bp = tile ? tile : (nimg <= 16 ? 16 : (nimg <= 32 ? 32 : 64));  // images per CTA
+        if (bp == 16) rc = launch_tc<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        else if (bp == 32) rc = launch_tc<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
         else rc = launch_tc<64>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
     } else {
         dim3 grid(nrows, (N + 31) / 32);

@@ -30,9 +30,9 @@ int adrt_adj(int dtype, int n, int nimg, const void* b, void* x, void* scratch, 
              const int* active = nullptr);
 int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                const void* p2, const double* x, const double* xp, double* xn, double om_a, double om_1, double a0,
-               int precond, int g1_deg, const double* g1_coef, const double* om_img, cudaStream_t st);
+               int precond, int g1_deg, const double* g1_coef, const double* om_img, int band, cudaStream_t st);
 int outer_step_max_n(int dtype);
 int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
-               void* Zd, int* err, int use_tc, cudaStream_t st);
+               void* Zd, int* err, int use_tc, int tile, cudaStream_t st);
 int cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, cudaStream_t st);
 }  // namespace adrt

@@ -218,10 +218,11 @@ static int launch_os_band(const OuterStepArgs& A, int nimg, cudaStream_t st) {
 // 32-row bands; when the batch's clusters cannot fill the SMs (N <= 256), 16-row bands instead: twice the CTAs per
 // image (clusters of up to 16), half the rows each, so a small batch finishes its stencil steps sooner
 template <typename TS, typename TP, int n>
-static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
+static int launch_os(const OuterStepArgs& A, int nimg, int band, cudaStream_t st) {
     constexpr int N = 1 << n;
     if constexpr (N >= 32 && N / 16 <= 16) {
-        if ((long)nimg * (N / 32) < device_sm_count()) return launch_os_band<TS, TP, n, 16>(A, nimg, st);
+        const bool b16 = band ? band == 16 : (long)nimg * (N / 32) < device_sm_count();
+        if (b16) return launch_os_band<TS, TP, n, 16>(A, nimg, st);
     }
     return launch_os_band<TS, TP, n, (N >= 32 ? 32 : N)>(A, nimg, st);
 }
@@ -231,18 +232,18 @@ static int launch_os(const OuterStepArgs& A, int nimg, cudaStream_t st) {
 int outer_step_max_n(int dtype) { return dtype == ADRT_F32 ? 9 : 8; }
 
 template <typename TS, typename TP>
-static int dispatch_os(int n, const OuterStepArgs& A, int nimg, cudaStream_t st) {
+static int dispatch_os(int n, const OuterStepArgs& A, int nimg, int band, cudaStream_t st) {
     switch (n) {
-        case 1: return launch_os<TS, TP, 1>(A, nimg, st);
-        case 2: return launch_os<TS, TP, 2>(A, nimg, st);
-        case 3: return launch_os<TS, TP, 3>(A, nimg, st);
-        case 4: return launch_os<TS, TP, 4>(A, nimg, st);
-        case 5: return launch_os<TS, TP, 5>(A, nimg, st);
-        case 6: return launch_os<TS, TP, 6>(A, nimg, st);
-        case 7: return launch_os<TS, TP, 7>(A, nimg, st);
-        case 8: return launch_os<TS, TP, 8>(A, nimg, st);
+        case 1: return launch_os<TS, TP, 1>(A, nimg, band, st);
+        case 2: return launch_os<TS, TP, 2>(A, nimg, band, st);
+        case 3: return launch_os<TS, TP, 3>(A, nimg, band, st);
+        case 4: return launch_os<TS, TP, 4>(A, nimg, band, st);
+        case 5: return launch_os<TS, TP, 5>(A, nimg, band, st);
+        case 6: return launch_os<TS, TP, 6>(A, nimg, band, st);
+        case 7: return launch_os<TS, TP, 7>(A, nimg, band, st);
+        case 8: return launch_os<TS, TP, 8>(A, nimg, band, st);
         case 9:
-            if constexpr (sizeof(TS) == 4) return launch_os<TS, TP, 9>(A, nimg, st);
+            if constexpr (sizeof(TS) == 4) return launch_os<TS, TP, 9>(A, nimg, band, st);
             break;
     }
     set_error("outer_step: n=%d unsupported for this stencil type", n);
@@ -251,7 +252,7 @@ static int dispatch_os(int n, const OuterStepArgs& A, int nimg, cudaStream_t st)
 
 int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                const void* p2, const double* x, const double* xp, double* xn, double om_a, double om_1, double a0,
-               int precond, int g1_deg, const double* g1_coef, const double* om_img, cudaStream_t st) {
+               int precond, int g1_deg, const double* g1_coef, const double* om_img, int band, cudaStream_t st) {
     const bool sd_ok = dtype == ADRT_F32 || dtype == ADRT_F64 || dtype == ADRT_F32X2;
     const bool pd_ok = parts_dtype == ADRT_F32 || parts_dtype == ADRT_F64;
     if (!sd_ok || !pd_ok || n < 1 || n > outer_step_max_n(dtype) || nimg < 0 || precond < 0 || precond > 2 ||
@@ -262,6 +263,7 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
     }
     if (!nimg) return ADRT_OK;
     if (!y || !xn || (om_img && !x)) { set_error("outer_step: null pointer"); return ADRT_EINVAL; }
+    if (band != 0 && band != 16 && band != 32) { set_error("outer_step: band must be 0 (auto), 16 or 32"); return ADRT_EINVAL; }
     OuterStepArgs A = {};
     A.y = y; A.p0 = p0; A.p1 = p1; A.p2 = p2; A.x = x; A.xp = xp; A.xn = xn;
     A.om_a = om_a; A.om_1 = om_1; A.a0 = a0; A.om_img = om_img; A.precond = precond; A.g1_deg = g1_deg;
@@ -275,12 +277,12 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
     // instantiated pairs: FP32 partial images with any stencil type, FP64 partial images with the FP64 stencil
     if (parts_dtype == ADRT_F32) {
         switch (dtype) {
-            case ADRT_F32: return dispatch_os<float, float>(n, A, nimg, st);
-            case ADRT_F64: return dispatch_os<double, float>(n, A, nimg, st);
-            default: return dispatch_os<ff, float>(n, A, nimg, st);
+            case ADRT_F32: return dispatch_os<float, float>(n, A, nimg, band, st);
+            case ADRT_F64: return dispatch_os<double, float>(n, A, nimg, band, st);
+            default: return dispatch_os<ff, float>(n, A, nimg, band, st);
         }
     }
-    if (dtype == ADRT_F64) return dispatch_os<double, double>(n, A, nimg, st);
+    if (dtype == ADRT_F64) return dispatch_os<double, double>(n, A, nimg, band, st);
     set_error("outer_step: FP64 partial images take the FP64 stencil only");
     return ADRT_EUNSUPPORTED;
 }

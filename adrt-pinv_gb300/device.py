@@ -65,6 +65,7 @@ class RowTables:
         # set by the owning pipeline before the first dense table is built
         self.stream_dense = False
         self.row_grid = 0  # CTAs of the row programs (0: one per SM); set by the autotuner
+        self.dense_tile = 0  # images per CTA of the tensor-core dense rows (0: from the batch); set by the autotuner
         self.err = torch.zeros(1, dtype=torch.int32, device=device)
         self._zd = None
         # compensated high rows: float-float kernel in an FP32 pipeline; an FP64 pipeline runs them as ordinary
@@ -172,7 +173,7 @@ class RowTables:
             self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
         mode = 2 if self.stream_dense else (1 if self.use_tc else 0)
         C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(T), C.ptr(Y), R * N,
-               C.ptr(self._zd), C.ptr(self.err), mode, C.stream_handle())
+               C.ptr(self._zd), C.ptr(self.err), mode, self.dense_tile if mode == 1 else 0, C.stream_handle())
 
     def run_ff(self, Y, ops):
         """The op list on the high-condition rows in float-float arithmetic (adrt_rows_ff_run)."""
@@ -350,6 +351,7 @@ class Pipeline:
         self.ops = _op_lists(plan)
         self.launches = 0
         self.timer = None  # list: when set, ("pack_image" | "pack_sino" | "unpack", start, end) CUDA events per launch
+        self.band = 0  # rows per CTA of the fused outer step (0: from the batch); set by the autotuner
 
     # ---------------------------------------------------------------- packed passes
     def _codes(self):
@@ -442,7 +444,8 @@ class Pipeline:
         parts = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
         C.call("adrt_outer_step", self.stencil_code, self._codes(), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
                C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
-               p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), C.stream_handle())
+               p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), self.band,
+               C.stream_handle())
 
     def outer_step(self, x, x_prev, r, x_new, om_a, om_1, a0, om_img=None):
         """x_new = x + om_a r + om_1 (x - x_prev) (x None: a0 r); om_img (device (B, 2) FP64, optional): per-image

@@ -1,10 +1,13 @@
-"""Autotuner for the launch configuration of a device pipeline.
+"""Autotuner for the launch configuration and tile shapes of a device pipeline.
 
-Per (plan, batch, precision) the tuner times the candidate configurations of the two choices that depend on the
+Per (plan, batch, precision) the tuner times the candidate configurations of the choices that depend on the
 workload's shape, on the GPU and with the pipeline's own data, and keeps the fastest:
   * the dense-row kernel: tensor cores (3xTF32 tcgen05), the streaming CUDA-core kernel (batches of at most 16; the
-    operators stored transposed) or the tiled CUDA-core kernel;
-  * the grid of the row programs: one or two persistent CTAs per SM.
+    operators stored transposed) or the tiled CUDA-core kernel, crossed with the grid of the row programs (one or
+    two persistent CTAs per SM);
+  * then, one dimension at a time with the others held at the best so far, the tile shapes: images per CTA of the
+    tensor-core dense kernel (16, 32, 64) and rows per CTA of the fused outer step's bands (16 or 32, which also
+    sets the cluster size, N/16 or N/32 CTAs per image).
 Each candidate is timed with CUDA events over `reps` applies after one warm-up apply. Results are cached per
 (N, method, degree cap, dense cap, batch, precision, GPU name) in memory and, when a path is given, in a JSON file.
 """
@@ -33,11 +36,24 @@ def candidates(pipe):
     return [{"dense": d, "row_grid": g} for d, g in itertools.product(dense, (sms, 2 * sms))]
 
 
+def tile_dimensions(pipe, cfg):
+    """The tile-shape choices worth timing for this pipeline once the kernels are chosen: {name: [values]}."""
+    dims = {}
+    if cfg.get("dense") == "tc":
+        dims["dense_tile"] = [16, 32, 64]
+    N = pipe.plan.N
+    if pipe.fused_outer_ok() and N >= 32 and N // 16 <= 16:
+        dims["band"] = [16, 32]
+    return dims
+
+
 def apply_config(pipe, cfg):
     t = pipe.tables
     t.stream_dense = cfg["dense"] == "stream"
     t.use_tc = cfg["dense"] == "tc"
     t.row_grid = int(cfg["row_grid"])
+    t.dense_tile = int(cfg.get("dense_tile", 0))
+    pipe.band = int(cfg.get("band", 0))
 
 
 def key_of(pipe):
@@ -71,11 +87,23 @@ class Tuner:
         k = key_of(pipe)
         if k not in self.cache:
             times = {}
+
+            def run(cfg):
+                key = json.dumps(cfg, sort_keys=True)
+                if key not in times:
+                    apply_config(pipe, cfg)
+                    times[key] = self.timer(pipe, b)
+                return times[key]
+
             for cfg in candidates(pipe):
-                apply_config(pipe, cfg)
-                times[json.dumps(cfg, sort_keys=True)] = self.timer(pipe, b)
-            best = min(times, key=times.get)
-            self.cache[k] = {"config": json.loads(best), "ms": times}
+                run(cfg)
+            best = json.loads(min(times, key=times.get))
+            for name, values in tile_dimensions(pipe, best).items():
+                for v in values:
+                    cfg = dict(best, **{name: v})
+                    if run(cfg) < run(best):
+                        best = cfg
+            self.cache[k] = {"config": best, "ms": times}
             if self.path:
                 with open(self.path, "w") as f:
                     json.dump(self.cache, f, indent=1)

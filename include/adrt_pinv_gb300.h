@@ -166,10 +166,12 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
  * image in shared memory for every stencil step. g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
  * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). om_img (nullable, DEVICE, with x given): per-image pairs
  * (om_a, om_1) that replace om_a and om_1, so that images at different outer iterations step together (slot-level
- * serving). Supported: n <= adrt_outer_step_max_n(dtype). */
+ * serving). band: rows of an image per CTA, 16 or 32 (0: chosen from the batch). Supported:
+ * n <= adrt_outer_step_max_n(dtype). */
 int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                     const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
-                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, void* stream);
+                    double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, int band,
+                    void* stream);
 int adrt_outer_step_max_n(int dtype);
 
 /* Dense low-frequency rows (fastops.py:28-40, 100-117): for r < nrows and every image b,
@@ -178,9 +180,10 @@ int adrt_outer_step_max_n(int dtype);
  * copied back. use_tc = 1 with FP32 and n >= 6: tensor cores (tcgen05.mma kind::tf32, 3xTF32 split, FP32 accumulate);
  * *err (device int) is set to 1 if a tensor-core completion wait ran out. use_tc = 2 (FP32, nimg <= 16): W is given
  * TRANSPOSED (W[r][i][o] = W_r[o][i]) and a CUDA-core kernel streams it once per group of 8 images (small batches,
- * where the product is bound by reading the operators). Otherwise (use_tc = 0) CUDA cores. */
+ * where the product is bound by reading the operators). Otherwise (use_tc = 0) CUDA cores. tile (tensor cores):
+ * images per CTA, 16, 32 or 64 (0: chosen from nimg). */
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
-                    long long img_stride, void* Zd, int32_t* err, int use_tc, void* stream);
+                    long long img_stride, void* Zd, int32_t* err, int use_tc, int tile, void* stream);
 
 /* Spatial ADRT in the reference's sinogram layout (adrtcore.py:122-137), nimg images, exact for integer dtypes
  * (ADRT_I32, ADRT_I64; sums only), FP32 / FP64 otherwise. scratch: 2 * nimg * 4 * (2N-1) * N elements of dtype.

@@ -22,14 +22,14 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
     ref = Y.copy()
     for i, r in enumerate(rows):
         ref[:, r, :] = Y[:, r, :] @ W[i].T
-    for use_tc in (1, 0):
+    for use_tc, tile in ((1, 0), (1, 16), (1, 64), (0, 0)):
         Wd = torch.from_numpy(W).to("cuda", torch.complex64)
         Yd = torch.from_numpy(Y).to("cuda", torch.complex64)
         rd = torch.from_numpy(rows).cuda()
         Zd = torch.empty((nrows, nimg, N), dtype=torch.complex64, device="cuda")
         err = torch.zeros(1, dtype=torch.int32, device="cuda")
         C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(Wd), C.ptr(Yd), R * N, C.ptr(Zd), C.ptr(err),
-               use_tc, C.stream_handle())
+               use_tc, tile, C.stream_handle())
         torch.cuda.synchronize()
         assert int(err.item()) == 0
         out = Yd.cpu().numpy()
@@ -41,7 +41,7 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
     Yd = torch.from_numpy(Y).cuda()
     Zd = torch.empty((nrows, nimg, N), dtype=torch.complex128, device="cuda")
     C.call("adrt_dense_rows", C.F64, n, nimg, nrows, C.ptr(torch.from_numpy(rows).cuda()), C.ptr(Wd), C.ptr(Yd), R * N,
-           C.ptr(Zd), None, 0, C.stream_handle())
+           C.ptr(Zd), None, 0, 0, C.stream_handle())
     torch.cuda.synchronize()
     assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
 
@@ -66,7 +66,7 @@ def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
     Yd = torch.from_numpy(Y).to("cuda", torch.complex64)
     rd = torch.from_numpy(rows).cuda()
     Zd = torch.empty((nrows, nimg, N), dtype=torch.complex64, device="cuda")
-    C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Yd), R * N, C.ptr(Zd), None, 2,
+    C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Yd), R * N, C.ptr(Zd), None, 2, 0,
            C.stream_handle())
     out = Yd.cpu().numpy()
     for r in range(R):
@@ -74,7 +74,7 @@ def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
         assert e < 1e-6, (r, e)
     Z9 = torch.empty((nrows, 17, N), dtype=torch.complex64, device="cuda")
     Y9 = torch.zeros((17, R, N), dtype=torch.complex64, device="cuda")
-    rc = C.load().adrt_dense_rows(C.F32, n, 17, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Y9), R * N, C.ptr(Z9), None, 2,
+    rc = C.load().adrt_dense_rows(C.F32, n, 17, nrows, C.ptr(rd), C.ptr(WT), C.ptr(Y9), R * N, C.ptr(Z9), None, 2, 0,
                                   C.stream_handle())
     assert rc != 0
 

@@ -120,6 +120,8 @@ def test_autotuned_pipeline_same_results(pkg, golden):
     ref = inv.pipeline(3).apply(bs).clone()
     pipe = Pipeline(inv.plan, 3, "fp32", "cuda")
     res = tune.Tuner(reps=1).tune(pipe, bs)
-    assert len(res["ms"]) == len(tune.candidates(pipe)) >= 2 and res["config"] in tune.candidates(pipe)
+    stage1 = tune.candidates(pipe)
+    assert len(res["ms"]) >= len(stage1) >= 2
+    assert {k: res["config"][k] for k in ("dense", "row_grid")} in stage1
     out = pipe.apply(bs)
     assert float((out - ref).norm() / ref.norm()) < 1e-6
