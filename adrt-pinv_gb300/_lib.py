@@ -75,6 +75,9 @@ PROTOTYPES = {
     "adrt_fp32_probe": [_I, _I, _I, _P, _P],
     "adrt_rows_run": [ctypes.POINTER(RowJob), _P],
     "adrt_rows_ff_run": [ctypes.POINTER(RowJob), _P],
+    "adrt_rows_multi_code": [ctypes.POINTER(RowJob)],
+    "adrt_rows_lanes_per_row": [_I],
+    "adrt_rows_run_multi": [_P, _P, _P, _I, _P, _I, _P],
     "adrt_twiddle_table": [_I, _I, _I, _P, _P, _P],
     "adrt_power_rows": [_I, _I, _I, _P, _P, _I, _I, _D, _P, _P, _P],
     "adrt_cert_rowsum_dev": [_I, _I, _P, _I, _P, _P],

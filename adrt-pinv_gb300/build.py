@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(REPO, "include")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libadrt_pinv_gb300.so")
-SOURCES = ["rows.cu", "fft.cu", "image.cu", "outer_step.cu", "adrt.cu", "cert.cu", "capi.cu", "noalloc.cu", "dense.cu", "cgls.cu", "rows_ff.cu"]
+SOURCES = ["rows.cu", "fft.cu", "image.cu", "outer_step.cu", "adrt.cu", "cert.cu", "capi.cu", "noalloc.cu", "dense.cu", "cgls.cu", "rows_ff.cu", "rows_multi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
 

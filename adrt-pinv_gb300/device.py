@@ -182,11 +182,17 @@ class RowTables:
         j.coef = self.coef64.data_ptr()
         C.call("adrt_rows_ff_run", ctypes.byref(j), C.stream_handle())
 
-    def run(self, Y, ops):
+    def main_job(self, Y, ops):
+        """The row job of the polynomial rows of one op list (what run() launches first), for a caller that launches
+        it itself (one persistent launch over several pipelines' rows)."""
+        return self.job(Y, fuse_ops(ops), self.rows_main)
+
+    def run(self, Y, ops, skip_main=False):
         """RowEngine.run (fastops.py:156-167) on device rows Y (B, 2L, N), in place. Dense rows take the exact
         filter (fastops.py:100-117), fused with the butterflies around it (adjoint levels before, Gram levels and
         the level-1 butterflies of the hybrid around it) into one precomputed operator per row; with compensated
-        high rows (plan.high_rows == "ff") they keep the polynomial filter in float-float arithmetic instead."""
+        high rows (plan.high_rows == "ff") they keep the polynomial filter in float-float arithmetic instead.
+        skip_main: the polynomial rows (main_job) were run by the caller; only the rest is done here."""
         ops = fuse_ops(ops)
         B = Y.shape[0]
         if not ops:
@@ -196,12 +202,18 @@ class RowTables:
         if len(pidx) > 1:
             raise ValueError("at most one filter op per list")
         dense = len(self.plan.dense_freqs) > 0
+        if skip_main and (not dense or not pidx):
+            if dense:  # no filter: the dense rows take the op list like the others
+                C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, self.rows_dense)), st)
+            self.count += B * self.plan.level_rows(ops_unfused(ops))
+            return
         if dense and self.high_poly:
             if self.high_ff:
-                self._timed_main(Y, ops, st)
+                if not skip_main:
+                    self._timed_main(Y, ops, st)
                 self.run_ff(Y, ops)
             else:
-                rows = torch.cat([self.rows_main, self.rows_dense])
+                rows = self.rows_dense if skip_main else torch.cat([self.rows_main, self.rows_dense])
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, ops, rows)), st)
             self.count += B * self.plan.level_rows(ops_unfused(ops))
             return
@@ -227,7 +239,8 @@ class RowTables:
                 pre = []
             if post_b1t:
                 post = []
-            self._timed_main(Y, ops, st)
+            if not skip_main:
+                self._timed_main(Y, ops, st)
             if pre:
                 C.call("adrt_rows_run", ctypes.byref(self.job(Y, pre, self.rows_dense)), st)
             self.dense_apply(Y, self.dense_table(fold_pre, fold_post, pre_b1, post_b1t))
@@ -352,6 +365,29 @@ class Pipeline:
         self.launches = 0
         self.timer = None  # list: when set, ("pack_image" | "pack_sino" | "unpack", start, end) CUDA events per launch
         self.band = 0  # rows per CTA of the fused outer step (0: from the batch); set by the autotuner
+
+    def prefix(self, b):
+        """A pipeline over the first b images of this one's buffers (views of the same memory; same plan, precision
+        and kernel choices, its own row-table state and dense-row staging): steps over a prefix of the batch cost in
+        proportion to b."""
+        b = int(b)
+        if not 1 <= b <= self.B:
+            raise ValueError("prefix size out of range")
+        q = object.__new__(Pipeline)
+        q.__dict__.update(self.__dict__)
+        q.B = b
+        t = RowTables(self.plan, self.real, self.device)
+        for k in ("stream_dense", "use_tc", "row_grid", "dense_tile"):
+            setattr(t, k, getattr(self.tables, k))
+        q.tables = t
+        q.Y = self.Y[:b]
+        q.parts = self.parts[:, :b]
+        q.xs = [x[:b] for x in self.xs]
+        q.y = self.y[:b]
+        q.s = self.s[:b]
+        q.st = [x[:b] for x in self.st]
+        q.timer = None
+        return q
 
     # ---------------------------------------------------------------- packed passes
     def _codes(self):
@@ -534,6 +570,26 @@ class Pipeline:
         self.tables.count += self.graph_count
         return self.x_out
 
+    def first_step(self, y, x_out, a):
+        """x_1 = a P(y) (P = identity for L_p): the outer iteration's first step (fastops.py:250)."""
+        if self.fused_outer_ok():
+            self.fused_outer_step(y, False, None, None, x_out, 0.0, 0.0, a)
+        elif self.plan.method == "hybrid":
+            r = self.precond(self.resid(y, with_parts=False))
+            self.outer_step(None, None, r, x_out, 0.0, 0.0, a)
+        else:
+            self.outer_step(None, None, y, x_out, 0.0, 0.0, a)
+
+    def next_step(self, y, x, x_prev, x_new, om_a, om_1):
+        """x_new = x + om_a P(y - G x) + om_1 (x - x_prev), with G x already in the partial images
+        (fastops.py:252-257)."""
+        if self.fused_outer_ok():
+            self.fused_outer_step(y, True, x, x_prev, x_new, om_a, om_1, 0.0)
+        else:
+            s = self.resid(y)
+            r = self.precond(s) if self.plan.method == "hybrid" else s
+            self.outer_step(x, x_prev, r, x_new, om_a, om_1, 0.0)
+
     def apply(self, b):
         """x = L b for B sinograms b (B, 4, 2N-1, N) on device; returns the FP64 (B, N, N) result buffer (a view
         of internal storage, valid until the next call)."""
@@ -542,30 +598,30 @@ class Pipeline:
             raise RuntimeError("plan has no outer interval")
         a, c, steps = outer_coeffs(p.lo, p.hi, p.outer_deg)
         y = self.backproject_into(b, self.y)
-        hybrid = p.method == "hybrid"
-        fused = self.fused_outer_ok()
         x, xp = self.xs[0], None
-        if fused:
-            self.fused_outer_step(y, False, None, None, x, 0.0, 0.0, a)
-        elif hybrid:
-            r = self.precond(self.resid(y, with_parts=False))
-            self.outer_step(None, None, r, x, 0.0, 0.0, a)
-        else:
-            self.outer_step(None, None, y, x, 0.0, 0.0, a)
+        self.first_step(y, x, a)
         free = [self.xs[1], self.xs[2]]
         for om_a, om_1 in steps:
             self.G(x)
             xn = free.pop(0)
-            if fused:
-                self.fused_outer_step(y, True, x, xp, xn, om_a, om_1, 0.0)
-            else:
-                s = self.resid(y)
-                r = self.precond(s) if hybrid else s
-                self.outer_step(x, xp, r, xn, om_a, om_1, 0.0)
+            self.next_step(y, x, xp, xn, om_a, om_1)
             if xp is not None:
                 free.append(xp)
             xp, x = x, xn
         return x
+
+    # ---------------------------------------------------------------- the stages around the row engine
+    def pack(self, src, sino):
+        """The pack + FFT kernel of one packed pass: sinograms (B, 4, 2N-1, N) or images (B, N, N) -> Y."""
+        p, st = self.plan, C.stream_handle()
+        C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1 if sino else 0, C.dtype_code(src.dtype), C.ptr(src),
+               C.ptr(self.Y), C.ptr(self.tables.roots), st)
+
+    def finish_pass(self, ops):
+        """Everything of a packed pass after the polynomial-row launch: the dense (or compensated) rows, the inverse
+        FFT and the unpack into the partial images."""
+        self.tables.run(self.Y, ops, skip_main=True)
+        self._unpack(C.stream_handle())
 
 
 def _op_lists(plan):

@@ -141,8 +141,12 @@ class SlotLane:
         self.D = D = int(plan.outer_deg)
         self.device = torch.device(device)
         self.stream = torch.cuda.Stream(device=self.device)
+        # step pipelines over prefixes of the slots (B/8, B/4, B/2, B): a step costs in proportion to the highest
+        # occupied slot, and admission fills the lowest free slot, so a lightly loaded lane runs small steps
+        self.sizes = sorted({max(1, self.slots >> k) for k in range(4)})
         with torch.cuda.stream(self.stream):
             self.pipe = Pipeline(plan, self.slots, inverse.precision, self.device, inverse.stencil_precision)
+            self.sub = {b: (self.pipe if b == self.slots else self.pipe.prefix(b)) for b in self.sizes}
             self.bp = Pipeline(plan, 1, inverse.precision, self.device, inverse.stencil_precision)
             a, _, steps = outer_coeffs(plan.lo, plan.hi, D)
             tab = [(a, 0.0)] + [tuple(st) for st in steps] + [(0.0, 0.0)]
@@ -153,17 +157,19 @@ class SlotLane:
                 x.zero_()
             self.pipe.y.zero_()
             self.b1 = torch.zeros((1, 4, 2 * N - 1, N), dtype=torch.float64, device=self.device)
-            self._step_eager(0)  # builds every table and kernel attribute before the capture
-            self._step_eager(1)
+            for b in self.sizes:  # builds every table and kernel attribute before the capture
+                self._step_eager(0, b)
+                self._step_eager(1, b)
             self.bp.backproject_into(self.b1, self.pipe.y[:1])
             self.pipe.y.zero_()
         self.stream.synchronize()
-        self.graphs = []
-        for ph in range(3):
-            g = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(g, stream=self.stream):
-                self._step_eager(ph)
-            self.graphs.append(g)
+        self.graphs = {}
+        for b in self.sizes:
+            for ph in range(3):
+                g = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(g, stream=self.stream):
+                    self._step_eager(ph, b)
+                self.graphs[(b, ph)] = g
         self.s = 0  # global step counter (the buffer rotation phase is s % 3)
         self.hk = [D] * self.slots  # host mirror of the per-slot iteration counters
         self.req = [None] * self.slots
@@ -173,29 +179,38 @@ class SlotLane:
         self.step_events = deque()  # completion events of the steps in flight (at most `depth`)
         self.depth = 2  # steps queued ahead: the GPU never waits for the host, an admission waits at most 2 steps
         self.steps_run = 0
+        self.step_sizes = {}  # prefix size -> steps run at it
 
     @staticmethod
     def estimate_bytes(inverse, slots):
-        """The slot pipeline, the batch-1 back-projection pipeline and the per-slot coefficient state."""
+        """The slot pipeline, the batch-1 back-projection pipeline, the prefix pipelines' dense-row staging and the
+        per-slot coefficient state."""
         p = inverse.plan
+        N, nd = p.N, 2 * len(p.dense_freqs)
+        rs = 4 if inverse.precision == "fp32" else 8
+        prefixes = sum(max(1, int(slots) >> k) for k in range(1, 4) if max(1, int(slots) >> k) < int(slots))
         return (Pipeline.estimate_bytes(p, slots, inverse.precision, inverse.stencil_precision, captured=False) +
                 Pipeline.estimate_bytes(p, 1, inverse.precision, inverse.stencil_precision, captured=True) +
-                int(slots) * 24 + (int(p.outer_deg) + 1) * 16)
+                nd * prefixes * N * 2 * rs + int(slots) * 24 + (int(p.outer_deg) + 1) * 16)
 
     def device_bytes(self):
+        zd = sum(q.tables._zd.numel() * q.tables._zd.element_size() for b, q in self.sub.items()
+                 if q is not self.pipe and q.tables._zd is not None)
         return (self.pipe.device_bytes() + self.bp.device_bytes() + self.b1.numel() * 8 + self.k.numel() * 8 +
-                self.om.numel() * 8 + self.coef_tab.numel() * 8)
+                self.om.numel() * 8 + self.coef_tab.numel() * 8 + zd)
 
-    def _bufs(self, ph):
-        xs = self.pipe.xs
+    def _bufs(self, ph, xs=None):
+        xs = self.pipe.xs if xs is None else xs
         return xs[ph % 3], xs[(ph + 2) % 3], xs[(ph + 1) % 3]  # cur, prev, new
 
-    def _step_eager(self, ph):
-        cur, prev, new = self._bufs(ph)
-        torch.index_select(self.coef_tab, 0, self.k, out=self.om)
-        self.pipe.G(cur)
-        self.pipe.step_all(self.pipe.y, cur, prev, new, self.om)
-        self.k.add_(1).clamp_(max=self.D)
+    def _step_eager(self, ph, b):
+        """One step of the first b slots (the others keep their state)."""
+        q = self.sub[b]
+        cur, prev, new = self._bufs(ph, q.xs)
+        torch.index_select(self.coef_tab, 0, self.k[:b], out=self.om[:b])
+        q.G(cur)
+        q.step_all(q.y, cur, prev, new, self.om[:b])
+        self.k[:b].add_(1).clamp_(max=self.D)
 
     # the server's lane interface
     def free_slots(self):
@@ -234,8 +249,11 @@ class SlotLane:
             self.step_events.popleft()
         if len(self.step_events) >= self.depth:
             return
+        top = max(i for i, r in enumerate(self.req) if r is not None) + 1
+        b = next(sz for sz in self.sizes if sz >= top)
         with torch.cuda.stream(self.stream):
-            self.graphs[self.s % 3].replay()
+            self.graphs[(b, self.s % 3)].replay()
+            self.step_sizes[b] = self.step_sizes.get(b, 0) + 1
             _, _, new = self._bufs(self.s)
             self.s += 1
             self.steps_run += 1
@@ -280,8 +298,9 @@ class SlotLane:
         return out
 
     def release(self):
-        self.graphs = []
+        self.graphs = {}
         self.pipe = self.bp = None
+        self.sub = {}
 
 
 class InverseServer:

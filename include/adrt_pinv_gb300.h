@@ -113,6 +113,17 @@ int adrt_rows_run(const adrt_row_job* job, void* stream);
  * FP64 (complex128) and `coef` the filter table in FP64; rows are read and written in FP32. */
 int adrt_rows_ff_run(const adrt_row_job* job, void* stream);
 
+/* Several row jobs in ONE persistent launch (the polynomial rows of many inverses of different N and op lists, e.g.
+ * the classes of an uneven batch; the reference runs one RowEngine.run per image, fastops.py:156-167). jobs: njobs
+ * DEVICE-resident job structs; code[j] = adrt_rows_multi_code(job j) (FP32, n = 6..9, a compile-time op list, a row
+ * selection, roots of unity; -1 when the job cannot join); wstart[j] = the first warp item of job j, wstart[njobs]
+ * the total, where job j has ceil(nimg * nsel / (32 / adrt_rows_lanes_per_row(n))) warp items (device int arrays).
+ * Every warp of the grid (0: one CTA per SM) takes warp items from the one counter (reset here). */
+int adrt_rows_multi_code(const adrt_row_job* job);
+int adrt_rows_lanes_per_row(int n);
+int adrt_rows_run_multi(const adrt_row_job* jobs, const int32_t* code, const int32_t* wstart, int njobs,
+                        int32_t* counter, int grid, void* stream);
+
 /* Per-row twiddle table tab[k*(N/2+1) + t] = z_k^t (t = 0..N/2) from K complex z (FP64 in, dtype out),
  * by binary powering in FP64. */
 int adrt_twiddle_table(int dtype, int n, int K, const double* z, void* tab, void* stream);

@@ -103,3 +103,37 @@ def test_n2048_hybrid_p64_batch1_vs_fp64(pkg):
     ref = H.pipeline(1, "fp64").apply(b.contiguous())[0].cpu().numpy()
     err = rel_err(got, ref)
     assert err < 1e-5, err
+
+
+def test_persistent_uneven_batch_matches_oracle(pkg):
+    """The uneven batch with every class's polynomial rows in one persistent launch per outer step (lock-step
+    classes, one CUDA graph): each sinogram against the oracle on its class's plan, and equal to the stream-per-class
+    graph to 1e-6 (same kernels but for the row launch)."""
+    import torch
+
+    from adrt_pinv_gb300 import uneven
+
+    classes = [(6, "lp", 8, 2), (6, "hybrid", 32, 3), (7, "lp", 16, 2), (7, "hybrid", 16, 2), (6, "hybrid", 8, 1)]
+    rng = np.random.default_rng(6)
+    groups, sinos, oracles = [], [], []
+    for n, method, p, count in classes:
+        cls = pkg.FastLpGpu if method == "lp" else pkg.FastHybridGpu
+        inv = cls(n, deg_cap=p, dense_cap=DENSE_CAP[p], precision="fp32")
+        groups.append((inv, count))
+        sinos.append(_sinos(pkg, n, count, 2000 * n + p, rng.uniform(1e-4, 1e-2, count)))
+        oracles.append(_oracle(inv, method, DENSE_CAP[p]))
+    P = uneven.PersistentUnevenBatch(groups)
+    U = uneven.UnevenBatch(groups)
+    dev = [torch.from_numpy(s).cuda() for s in sinos]
+    P.set_inputs(dev)
+    U.set_inputs(dev)
+    for _ in range(2):
+        outs = [o.clone() for o in P.replay()]
+        ref = [o.clone() for o in U.replay()]
+        torch.cuda.synchronize()
+        P.check()
+        for (n, method, p, count), o, r, s, orc in zip(classes, outs, ref, sinos, oracles):
+            assert float((o - r).norm() / r.norm()) < 1e-6, (n, method, p)
+            got = o.cpu().numpy()
+            for i in range(count):
+                assert rel_err(got[i], orc.apply(s[i])) < 1e-5, (n, method, p, i)
