@@ -81,8 +81,8 @@ PROTOTYPES = {
     "adrt_twiddle_table": [_I, _I, _I, _P, _P, _P],
     "adrt_power_rows": [_I, _I, _I, _P, _P, _I, _I, _D, _P, _P, _P],
     "adrt_cert_rowsum_dev": [_I, _I, _P, _I, _P, _P],
-    "adrt_pack_fft": [_I, _I, _I, _I, _I, _P, _P, _P, _P],
-    "adrt_ifft_unpack": [_I, _I, _I, _P, _P, _P, _P, _P, _P],
+    "adrt_pack_fft": [_I, _I, _I, _I, _I, _P, _P, _P, _I, _P],
+    "adrt_ifft_unpack": [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P],
     "adrt_resid": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P],
     "adrt_g1_step": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _P],
     "adrt_lorr": [_I, _I, _I, _P, _P, _P],

@@ -238,13 +238,13 @@ int adrt_cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* ou
 }
 
 int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-                  void* stream) {
-    return pack_fft(dtype, n, nimg, src_kind, src_dtype, src, Y, roots, as_stream(stream));
+                  int cols, void* stream) {
+    return pack_fft(dtype, n, nimg, src_kind, src_dtype, src, Y, roots, cols, as_stream(stream));
 }
 
 int adrt_ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* rowpart0, void* rowpart3,
-                     const void* roots, void* stream) {
-    return ifft_unpack(dtype, n, nimg, Z, colpart, rowpart0, rowpart3, roots, as_stream(stream));
+                     const void* roots, int cols, void* stream) {
+    return ifft_unpack(dtype, n, nimg, Z, colpart, rowpart0, rowpart3, roots, cols, as_stream(stream));
 }
 
 int adrt_resid(int dtype, int n, int nimg, int ydtype, const void* y, const void* p0, const void* p1, const void* p2,

@@ -83,13 +83,20 @@ __device__ __forceinline__ void dit_passes(cplx<real> (&x)[FftCfg<l>::E], const 
     }
 }
 
-template <typename real, int l, typename SRC>
-__global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) pack_fft_kernel(int nimg, int src_kind, const SRC* __restrict__ src,
-                                                        cplx<real>* __restrict__ Y, const cplx<real>* __restrict__ roots_g) {
+// threads of a CTA and the CTAs per SM the register budget is sized for (the whole SM's 2048 threads in FP32)
+template <typename real, int l, int CB> struct FftLaunch {
+    static constexpr int threads = CB * FftCfg<l>::TPC;
+    static constexpr int pack_min = sizeof(real) == 4 ? imax(1, 2048 / threads) : imax(1, 1024 / threads);
+    static constexpr int unpack_min = imax(1, 1024 / threads);
+};
+
+template <typename real, int l, int CB, typename SRC>
+__global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<real, l, CB>::pack_min)
+    pack_fft_kernel(int nimg, int src_kind, const SRC* __restrict__ src, cplx<real>* __restrict__ Y,
+                    const cplx<real>* __restrict__ roots_g) {
     using F = FftCfg<l>;
     using C = cplx<real>;
     constexpr int L = F::L, N = L / 2;
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
     constexpr int CP = fft_pad(CB);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* roots = reinterpret_cast<C*>(smem_raw);
@@ -172,14 +179,13 @@ __global__ void __launch_bounds__(1024, sizeof(real) == 4 ? 2 : 1) pack_fft_kern
     for (int j = 0; j < F::E; ++j) out[(size_t)F::pos(F::NPASS - 1, t, j) * N] = x[j];
 }
 
-template <typename real, int l>
-__global__ void __launch_bounds__(1024) ifft_unpack_kernel(int nimg, const cplx<real>* __restrict__ Z, real* __restrict__ colpart,
-                                                           real* __restrict__ row0, real* __restrict__ row3,
-                                                           const cplx<real>* __restrict__ roots_g) {
+template <typename real, int l, int CB>
+__global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<real, l, CB>::unpack_min)
+    ifft_unpack_kernel(int nimg, const cplx<real>* __restrict__ Z, real* __restrict__ colpart, real* __restrict__ row0,
+                       real* __restrict__ row3, const cplx<real>* __restrict__ roots_g) {
     using F = FftCfg<l>;
     using C = cplx<real>;
     constexpr int L = F::L, N = L / 2;
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
     constexpr int CP = fft_pad(CB);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* roots = reinterpret_cast<C*>(smem_raw);
@@ -222,21 +228,23 @@ __global__ void __launch_bounds__(1024) ifft_unpack_kernel(int nimg, const cplx<
     }
 }
 
-template <typename real, int l> static size_t pack_smem() {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+template <typename real, int l, int CB> static size_t pack_smem() {
     return ((size_t)(1 << l) + (size_t)(1 << l) * fft_pad(CB)) * sizeof(cplx<real>);
 }
-template <typename real, int l> static size_t unpack_smem() {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+template <typename real, int l, int CB> static size_t unpack_smem() {
     return ((size_t)(1 << l) + ((size_t)(1 << l) + (size_t)(1 << (l - 1))) * fft_pad(CB)) * sizeof(cplx<real>);
 }
 
-template <typename real, int l, typename SRC>
-static int launch_pack_src(int nimg, int src_kind, const void* src, void* Y, const void* roots, cudaStream_t st) {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+// columns per CTA: the default (as many as fit, up to 16 FP32 / 8 FP64) or a quarter of it (narrower CTAs, more of
+// them per SM, so the load, transform and store phases of different CTAs overlap); cols = 0 picks the default
+template <typename real, int l> constexpr int cols_wide() { return fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>)); }
+template <typename real, int l> constexpr int cols_narrow() { return imax(1, cols_wide<real, l>() / 4); }
+
+template <typename real, int l, int CB, typename SRC>
+static int launch_pack_cb(int nimg, int src_kind, const void* src, void* Y, const void* roots, cudaStream_t st) {
     constexpr int N = 1 << (l - 1);
-    const size_t smem = pack_smem<real, l>();
-    auto kern = pack_fft_kernel<real, l, SRC>;
+    const size_t smem = pack_smem<real, l, CB>();
+    auto kern = pack_fft_kernel<real, l, CB, SRC>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(N / CB, 2, nimg);
     kern<<<grid, CB * FftCfg<l>::TPC, smem, st>>>(nimg, src_kind, reinterpret_cast<const SRC*>(src),
@@ -245,24 +253,45 @@ static int launch_pack_src(int nimg, int src_kind, const void* src, void* Y, con
     return launch_status("pack_fft_kernel");
 }
 
-template <typename real, int l>
-static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, cudaStream_t st) {
-    if (src_dtype == ADRT_F64) return launch_pack_src<real, l, double>(nimg, src_kind, src, Y, roots, st);
-    return launch_pack_src<real, l, float>(nimg, src_kind, src, Y, roots, st);
+template <typename real, int l, typename SRC>
+static int launch_pack_src(int nimg, int src_kind, const void* src, void* Y, const void* roots, int cols,
+                           cudaStream_t st) {
+    constexpr int W = cols_wide<real, l>(), NW = cols_narrow<real, l>();
+    if (cols == 0 || cols == W) return launch_pack_cb<real, l, W, SRC>(nimg, src_kind, src, Y, roots, st);
+    if (NW != W && cols == NW) return launch_pack_cb<real, l, NW, SRC>(nimg, src_kind, src, Y, roots, st);
+    set_error("pack_fft: %d columns per CTA unsupported (%d or %d at n=%d)", cols, W, NW, l - 1);
+    return ADRT_EINVAL;
 }
 
 template <typename real, int l>
-static int launch_unpack(int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots, cudaStream_t st) {
-    constexpr int CB = fft_cols<l>(FftMax<real>::C, sizeof(cplx<real>));
+static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, int cols,
+                       cudaStream_t st) {
+    if (src_dtype == ADRT_F64) return launch_pack_src<real, l, double>(nimg, src_kind, src, Y, roots, cols, st);
+    return launch_pack_src<real, l, float>(nimg, src_kind, src, Y, roots, cols, st);
+}
+
+template <typename real, int l, int CB>
+static int launch_unpack_cb(int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots,
+                            cudaStream_t st) {
     constexpr int N = 1 << (l - 1);
-    const size_t smem = unpack_smem<real, l>();
-    auto kern = ifft_unpack_kernel<real, l>;
+    const size_t smem = unpack_smem<real, l, CB>();
+    auto kern = ifft_unpack_kernel<real, l, CB>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(N / CB, nimg);
     kern<<<grid, CB * FftCfg<l>::TPC, smem, st>>>(nimg, reinterpret_cast<const cplx<real>*>(Z), reinterpret_cast<real*>(colpart),
                                                    reinterpret_cast<real*>(row0), reinterpret_cast<real*>(row3),
                                                    reinterpret_cast<const cplx<real>*>(roots));
     return launch_status("ifft_unpack_kernel");
+}
+
+template <typename real, int l>
+static int launch_unpack(int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots, int cols,
+                         cudaStream_t st) {
+    constexpr int W = cols_wide<real, l>(), NW = cols_narrow<real, l>();
+    if (cols == 0 || cols == W) return launch_unpack_cb<real, l, W>(nimg, Z, colpart, row0, row3, roots, st);
+    if (NW != W && cols == NW) return launch_unpack_cb<real, l, NW>(nimg, Z, colpart, row0, row3, roots, st);
+    set_error("ifft_unpack: %d columns per CTA unsupported (%d or %d at n=%d)", cols, W, NW, l - 1);
+    return ADRT_EINVAL;
 }
 
 #define ADRT_FFT_CASES(F, ...)                     \
@@ -281,41 +310,43 @@ static int launch_unpack(int nimg, const void* Z, void* colpart, void* row0, voi
     }
 
 template <typename real>
-static int pack_t(int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, cudaStream_t st) {
-    ADRT_FFT_CASES(launch_pack, nimg, src_kind, src_dtype, src, Y, roots, st)
+static int pack_t(int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, int cols,
+                  cudaStream_t st) {
+    ADRT_FFT_CASES(launch_pack, nimg, src_kind, src_dtype, src, Y, roots, cols, st)
     set_error("pack_fft: n=%d unsupported", n);
     return ADRT_EUNSUPPORTED;
 }
 template <typename real>
-static int unpack_t(int n, int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots, cudaStream_t st) {
-    ADRT_FFT_CASES(launch_unpack, nimg, Z, colpart, row0, row3, roots, st)
+static int unpack_t(int n, int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots, int cols,
+                    cudaStream_t st) {
+    ADRT_FFT_CASES(launch_unpack, nimg, Z, colpart, row0, row3, roots, cols, st)
     set_error("ifft_unpack: n=%d unsupported", n);
     return ADRT_EUNSUPPORTED;
 }
 
 int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-             cudaStream_t st) {
+             int cols, cudaStream_t st) {
     if (n < 1 || n > 11 || nimg < 0 || (src_kind != 0 && src_kind != 1) ||
         (src_dtype != ADRT_F32 && src_dtype != ADRT_F64) || (nimg && (!src || !Y || !roots))) {
         set_error("pack_fft: bad arguments (n=%d nimg=%d src_kind=%d src_dtype=%d)", n, nimg, src_kind, src_dtype);
         return ADRT_EINVAL;
     }
     if (!nimg) return ADRT_OK;
-    if (dtype == ADRT_F32) return pack_t<float>(n, nimg, src_kind, src_dtype, src, Y, roots, st);
-    if (dtype == ADRT_F64) return pack_t<double>(n, nimg, src_kind, src_dtype, src, Y, roots, st);
+    if (dtype == ADRT_F32) return pack_t<float>(n, nimg, src_kind, src_dtype, src, Y, roots, cols, st);
+    if (dtype == ADRT_F64) return pack_t<double>(n, nimg, src_kind, src_dtype, src, Y, roots, cols, st);
     set_error("pack_fft: dtype must be F32 or F64");
     return ADRT_EINVAL;
 }
 
 int ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots,
-                cudaStream_t st) {
+                int cols, cudaStream_t st) {
     if (n < 1 || n > 11 || nimg < 0 || (nimg && (!Z || !colpart || !row0 || !row3 || !roots))) {
         set_error("ifft_unpack: bad arguments (n=%d nimg=%d)", n, nimg);
         return ADRT_EINVAL;
     }
     if (!nimg) return ADRT_OK;
-    if (dtype == ADRT_F32) return unpack_t<float>(n, nimg, Z, colpart, row0, row3, roots, st);
-    if (dtype == ADRT_F64) return unpack_t<double>(n, nimg, Z, colpart, row0, row3, roots, st);
+    if (dtype == ADRT_F32) return unpack_t<float>(n, nimg, Z, colpart, row0, row3, roots, cols, st);
+    if (dtype == ADRT_F64) return unpack_t<double>(n, nimg, Z, colpart, row0, row3, roots, cols, st);
     set_error("ifft_unpack: dtype must be F32 or F64");
     return ADRT_EINVAL;
 }

@@ -9,9 +9,9 @@ int device_sm_count();
 int rows_run(const adrt_row_job* J, int power_iters, double power_safety, double* power_out, cudaStream_t st);
 int twiddle_table(int dtype, int n, int K, const double* z, void* tab, cudaStream_t st);
 int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-             cudaStream_t st);
+             int cols, cudaStream_t st);
 int ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots,
-                cudaStream_t st);
+                int cols, cudaStream_t st);
 int image_resid(int dtype, int n, int nimg, int ydtype, const void* y, const void* p0, const void* p1, const void* p2,
                 void* s, cudaStream_t st);
 int image_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const void* p2, void* out, int out_dtype,

@@ -365,6 +365,7 @@ class Pipeline:
         self.launches = 0
         self.timer = None  # list: when set, ("pack_image" | "pack_sino" | "unpack", start, end) CUDA events per launch
         self.band = 0  # rows per CTA of the fused outer step (0: from the batch); set by the autotuner
+        self.fft_cols = 0  # strip columns per CTA of the offset FFTs (0: the default); set by the autotuner
 
     def prefix(self, b):
         """A pipeline over the first b images of this one's buffers (views of the same memory; same plan, precision
@@ -407,7 +408,8 @@ class Pipeline:
         """fastops._packed with strips Tq(q, E x): x (B, N, N) real on device -> self.parts."""
         p, st = self.plan, C.stream_handle()
         self._timed("pack_image", lambda: C.call("adrt_pack_fft", self._codes(), p.n, self.B, 0, C.dtype_code(x.dtype),
-                                                 C.ptr(x), C.ptr(self.Y), C.ptr(self.tables.roots), st))
+                                                 C.ptr(x), C.ptr(self.Y), C.ptr(self.tables.roots), self.fft_cols,
+                                                 st))
         self.tables.run(self.Y, ops)
         self._unpack(st)
         return self.parts
@@ -416,7 +418,7 @@ class Pipeline:
         """fastops._packed with strips iota(b_q): b (B, 4, 2N-1, N) real on device -> self.parts."""
         p, st = self.plan, C.stream_handle()
         C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1, C.dtype_code(b.dtype), C.ptr(b), C.ptr(self.Y),
-               C.ptr(self.tables.roots), st)
+               C.ptr(self.tables.roots), self.fft_cols, st)
         self.tables.run(self.Y, ops)
         self._unpack(st)
         return self.parts
@@ -424,7 +426,7 @@ class Pipeline:
     def _unpack(self, st):
         self._timed("unpack", lambda: C.call("adrt_ifft_unpack", self._codes(), self.plan.n, self.B, C.ptr(self.Y),
                                              C.ptr(self.parts[0]), C.ptr(self.parts[1]), C.ptr(self.parts[2]),
-                                             C.ptr(self.tables.roots), st))
+                                             C.ptr(self.tables.roots), self.fft_cols, st))
 
     def sum_parts(self, out):
         C.call("adrt_sum3", self._codes(), self.plan.n, self.B, C.ptr(self.parts[0]), C.ptr(self.parts[1]),
@@ -615,7 +617,7 @@ class Pipeline:
         """The pack + FFT kernel of one packed pass: sinograms (B, 4, 2N-1, N) or images (B, N, N) -> Y."""
         p, st = self.plan, C.stream_handle()
         C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1 if sino else 0, C.dtype_code(src.dtype), C.ptr(src),
-               C.ptr(self.Y), C.ptr(self.tables.roots), st)
+               C.ptr(self.Y), C.ptr(self.tables.roots), self.fft_cols, st)
 
     def finish_pass(self, ops):
         """Everything of a packed pass after the polynomial-row launch: the dense (or compensated) rows, the inverse

@@ -6,8 +6,9 @@ workload's shape, on the GPU and with the pipeline's own data, and keeps the fas
     operators stored transposed) or the tiled CUDA-core kernel, crossed with the grid of the row programs (one or
     two persistent CTAs per SM);
   * then, one dimension at a time with the others held at the best so far, the tile shapes: images per CTA of the
-    tensor-core dense kernel (16, 32, 64) and rows per CTA of the fused outer step's bands (16 or 32, which also
-    sets the cluster size, N/16 or N/32 CTAs per image).
+    tensor-core dense kernel (16, 32, 64), rows per CTA of the fused outer step's bands (16 or 32, which also
+    sets the cluster size, N/16 or N/32 CTAs per image) and strip columns per CTA of the offset FFTs (the default
+    or a quarter of it).
 Each candidate is timed with CUDA events over `reps` applies after one warm-up apply. Results are cached per
 (N, method, degree cap, dense cap, batch, precision, GPU name) in memory and, when a path is given, in a JSON file.
 """
@@ -44,7 +45,23 @@ def tile_dimensions(pipe, cfg):
     N = pipe.plan.N
     if pipe.fused_outer_ok() and N >= 32 and N // 16 <= 16:
         dims["band"] = [16, 32]
+    wide = fft_cols_default(N, pipe.real)
+    if wide >= 4:
+        dims["fft_cols"] = [wide, wide // 4]
     return dims
+
+
+def fft_cols_default(N, real):
+    """The offset FFTs' default strip columns per CTA (csrc/fft.cu fft_cols): up to 16 (FP32) / 8 (FP64), at most
+    1024 threads (8 points each along the 2N-long axis), at most N/2, and within 227 KB of shared memory."""
+    L = 2 * N
+    elem = 8 if real == torch.float32 else 16
+    tpc = L // 8 if L >= 8 else 1  # threads per column: 8 points each
+    c = max(1, min(16 if real == torch.float32 else 8, 1024 // tpc, N))
+    pad = lambda c: c + 1 if c > 1 else 1
+    while c > 1 and (L + (L + L // 2) * pad(c)) * elem > 227 * 1024:
+        c >>= 1
+    return c
 
 
 def apply_config(pipe, cfg):
@@ -54,6 +71,7 @@ def apply_config(pipe, cfg):
     t.row_grid = int(cfg["row_grid"])
     t.dense_tile = int(cfg.get("dense_tile", 0))
     pipe.band = int(cfg.get("band", 0))
+    pipe.fft_cols = int(cfg.get("fft_cols", 0))
 
 
 def key_of(pipe):

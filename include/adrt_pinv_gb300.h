@@ -143,13 +143,15 @@ int adrt_cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* ou
  * (fastspec.py:142-152); src_kind 1: src is nimg sinograms 4 x (2N-1) x N, strips = iota(b_q) (fastspec.py:170-174).
  * roots: L roots of unity in dtype. */
 int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-                  void* stream);
+                  int cols, void* stream);
 
 /* Inverse FFT along the offset axis + unpacking (fastops.py:216-220): from Z (nimg x 2L x N complex) produce the
  * three image-space partial sums whose total is E^T sum_q T_q^T Re/Im(ifft Z) (fastspec.py:154-168):
  * colpart (quadrants II, III), rowpart0 (quadrant I) and rowpart3 (quadrant IV), each nimg x N x N, dtype real. */
 int adrt_ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* rowpart0, void* rowpart3,
-                     const void* roots, void* stream);
+                     const void* roots, int cols, void* stream);
+/* cols (both): strip columns per CTA, 0 for the default (as many as fit, up to 16 in FP32 and 8 in FP64) or a
+ * quarter of the default (narrower CTAs, more of them per SM); other values are rejected. */
 
 /* Image-space kernels on nimg N x N images (dtype = ADRT_F32 / ADRT_F64 for all image arguments).
  * resid:   s = y - (p0 + p1 + p2)  (y in ydtype; parts in dtype, all NULL = 0, which casts y; s in dtype)

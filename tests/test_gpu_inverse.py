@@ -260,3 +260,25 @@ def test_compensated_rows_match_fp64_rows(pkg, method):
         t32.run(got, ops)
         err = ((got.to(torch.complex128) - ref)[:, rows].abs().max() / ref[:, rows].abs().max()).item()
         assert err < 2e-6, (ops, err)
+
+
+@pytest.mark.parametrize("n", [6, 8, 9])
+def test_fft_narrow_columns_same_result(pkg, n):
+    """The offset FFTs with a quarter of the default strip columns per CTA (a tile shape the autotuner may pick) give
+    the same packed pass: every column is transformed by the same arithmetic whatever the CTA shape."""
+    import torch
+
+    from adrt_pinv_gb300 import tune
+
+    N = 1 << n
+    plan = pkg.Plan("hybrid", n, np.full(2 * N, 4.0), outer=(1.0, 2.0, 3))
+    x = torch.randn((3, N, N), dtype=torch.float64, device="cuda", generator=torch.Generator("cuda").manual_seed(n))
+    outs = []
+    for cols in (0, tune.fft_cols_default(N, torch.float32) // 4):
+        pipe = pkg.Pipeline(plan, 3, "fp32")
+        pipe.fft_cols = cols
+        pipe.packed_image(x, [("B", 1, n), ("BT", 1, n)])
+        out = torch.empty_like(x)
+        pipe.sum_parts(out)
+        outs.append(out)
+    assert torch.equal(outs[0], outs[1])

@@ -66,4 +66,6 @@ def test_tile_shapes_of_the_tensor_core_kernel(pkg, monkeypatch):
     res = tune.Tuner(timer=timer).tune(p, None)
     assert res["config"] == {"dense": "tc", "row_grid": 152, "dense_tile": 32}  # band: no gain over the default
     assert p.tables.dense_tile == 32 and p.band == 0
-    assert tune.tile_dimensions(p, {"dense": "tc"}) == {"dense_tile": [16, 32, 64], "band": [16, 32]}
+    assert tune.tile_dimensions(p, {"dense": "tc"}) == {"dense_tile": [16, 32, 64], "band": [16, 32],
+                                                        "fft_cols": [16, 4]}
+    assert [tune.fft_cols_default(1 << n, torch.float32) for n in (2, 5, 8, 9, 10, 11)] == [4, 16, 16, 8, 4, 2]
