@@ -413,6 +413,7 @@ def run_ours(args):
         other = "ff" if args.stencil != "ff" else "fp32"
         line[f"preconditioner_{other}"] = stencil_variant(pkg, H, b_dev, args.steps, other, ref, torch)
         line["adrt_int32"] = adrt_int32_timing(pkg, n, B, args.steps, torch)
+        line["cgls"] = cgls_timing(pkg, n, 16, 50, torch)
         line.update(extras(pkg, dev, args))
     print(json.dumps(line), flush=True)
     if world > 1:
@@ -466,6 +467,39 @@ def adrt_int32_timing(pkg, n, B, steps, torch):
                                                      A.adrt_T(n, b[0].cpu().numpy(), dtype=np.int64)))
     out["workload"] = f"{B} int32 images N={N}, values U[0,255]"
     return out
+
+
+def cgls_timing(pkg, n, B, iters, torch):
+    """CGLS (pinv.py:23-48) on B noisy phantom sinograms at N = 2^n for a fixed number of iterations (tol = 0, so
+    no image stops): iterations per second and the HBM rate of an iteration, counting per image the spatial ADRT
+    and its transpose in FP64 (every level pass reads its input and writes its output) plus the vector passes (two
+    inner products, the x/r update and the direction update)."""
+    from adrt_pinv_gb300 import pinv
+
+    N = 1 << n
+    dev = torch.device("cuda")
+    b = _phantom_sinos(pkg, n, B, 4242, dev, REL_SIGMA)
+    S = pinv.CglsSolver(n, B, maxit=iters + 2, tol=0.0, device=dev, block=iters)
+    S.start(b)
+    S.iterate(2)  # warm-up
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    S.iterate(iters)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / iters
+    lvl = lambda m: 4 * (N + (1 << m) - 1) * N * 8
+    adrt_bytes = N * N * 8 + sum(lvl(m) for m in range(1, n + 1)) + sum(lvl(m) for m in range(1, n))
+    sino, img = 4 * (2 * N - 1) * N * 8, N * N * 8
+    vec_bytes = sino + img + (2 * img + 2 * sino) + (2 * img + img) + img  # <q,q>, <s,s>, x/r update, p update
+    per_iter = B * (2 * adrt_bytes + vec_bytes)
+    peak, _ = measured_hbm_peak()
+    gbs = per_iter / (ms * 1e-3) / 1e9
+    its = int(S.it[0].item())
+    return {"workload": f"CGLS on {B} sinograms N={N}, {iters} iterations (tol 0), FP64",
+            "ms_per_iteration": ms, "image_iterations_per_s": B / (ms * 1e-3), "bytes_per_iteration": per_iter,
+            "achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak, "iterations_run": its}
 
 
 def stencil_variant(pkg, H, b_dev, steps, stencil, ref, torch):

@@ -98,3 +98,31 @@ def test_gpu_gram_rejects_int_and_bad_intervals(pkg):
         pkg.gram.gram_freq(np.zeros((4, 8), dtype=np.complex128), np.zeros(4, dtype=np.float32))
     with pytest.raises(ValueError):
         pkg.gram.gram_freq(np.zeros((4, 8), dtype=np.complex128), np.zeros(5))
+
+
+def test_cgls_history_depends_on_summation_order(g):
+    """Why the GPU CGLS tests compare solutions and early histories only: the reference's own algorithm, run with its
+    inner products summed in another order (blocks of 37 terms), keeps the solution (<= 1e-7) and the history while
+    the residual is above 1e-3 of its start, then the histories part (by tens of percent mid-run) and the stopping
+    iteration can move by one."""
+    orig = P._ip
+
+    def blocked(a, c):
+        v = (np.asarray(a) * np.asarray(c)).ravel()
+        return float(sum(np.sum(v[i:i + 37]) for i in range(0, len(v), 37)))
+
+    worst_mid = 0.0
+    try:
+        P._ip = blocked
+        for key, tol, mx in (("4_2000", 1e-10, 2000), ("5_2000", 1e-8, 2000), ("6_3000", 1e-8, 3000)):
+            x, h = P.cgls(int(key[0]), g[f"cgls_b_{key}"], tol=tol, maxit=mx)
+            ref_h = g[f"cgls_hist_{key}"]
+            m = min(len(h), len(ref_h))
+            keep = ref_h[:m] > 1e-3 * ref_h[0]
+            rel = np.abs(h[:m] - ref_h[:m]) / ref_h[:m]
+            assert rel_err(x, g[f"cgls_x_{key}"]) < 1e-7 and rel[keep].max() < 1e-6
+            assert abs(len(h) - len(ref_h)) <= 2
+            worst_mid = max(worst_mid, rel.max())
+    finally:
+        P._ip = orig
+    assert worst_mid > 1e-2  # the later history is not reproducible at any fixed tolerance
