@@ -86,6 +86,122 @@ __global__ void adrt_adj_level(int n, int m, int nimg, const T* __restrict__ src
     }
 }
 
+// ------------------------------------------------------------------ tiled level passes (N >= 32, level m >= 2)
+// The per-element kernels above read the second term f(h + t + b, c1) along a shear: neighbouring output columns
+// read different rows, so a warp's loads touch many rows. The tiled passes stage the input rows a tile of 32 output
+// columns x ADRT_TR output rows needs in shared memory with row-contiguous (coalesced) loads, then gather from there;
+// the arithmetic and the guards are those of adrt_fwd_level / adj_at.
+constexpr int ADRT_TR = 32;  // output rows per tile
+
+template <typename T>
+__global__ void __launch_bounds__(256) adrt_fwd_level_tiled(int n, int m, const T* __restrict__ src,
+                                                            T* __restrict__ dst, size_t S,
+                                                            const int* __restrict__ active) {
+    const int N = 1 << n, w = 1 << (m - 1);
+    const int Hout = N + 2 * w - 1, off = w - 1;
+    const int s0 = blockIdx.x * 32, row0 = blockIdx.y * ADRT_TR;
+    const size_t slot = blockIdx.z;
+    if (active && !active[slot >> 2]) return;
+    const T* f = src + slot * S;
+    T* g = dst + slot * S;
+    const int h0 = row0 - (2 * w - 1);  // h of the tile's first output row
+    __shared__ T tA[ADRT_TR + 16][33];
+    __shared__ T tB[ADRT_TR + 16][17];
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    auto ld = [&](int h, int c) -> T { return (h >= -(w - 1) && h < N) ? f[(size_t)(h + off) * N + c] : (T)0; };
+    const bool small = 2 * w <= 32;
+    int cA = s0, cB = 0, hB = h0, t0 = 0;
+    if (small) {
+        // the 32 output columns read input columns of the same window, rows h0 .. h0 + TR + w - 1
+        for (int e = threadIdx.x; e < (ADRT_TR + w) * 32; e += 256) {
+            const int r = e >> 5, c = e & 31;
+            tA[r][c] = ld(h0 + r, s0 + c);
+        }
+    } else {
+        const int l = s0 / (2 * w);
+        t0 = (s0 - l * 2 * w) >> 1;
+        cA = l * 2 * w + t0;  // c0 columns cA .. cA + 15
+        cB = cA + w;          // c1 columns cB .. cB + 15
+        hB = h0 + t0;         // c1 rows h + t + b start at h0 + t0
+        for (int e = threadIdx.x; e < ADRT_TR * 16; e += 256) {
+            const int r = e >> 4, c = e & 15;
+            tA[r][c] = ld(h0 + r, cA + c);
+        }
+        for (int e = threadIdx.x; e < (ADRT_TR + 16) * 16; e += 256) {
+            const int r = e >> 4, c = e & 15;
+            tB[r][c] = ld(hB + r, cB + c);
+        }
+    }
+    __syncthreads();
+    const int s = s0 + lane;
+    const int l = s / (2 * w), rr = s - l * 2 * w, t = rr >> 1, b = rr & 1;
+    const int c0 = l * 2 * w + t, c1 = c0 + w;
+    for (int i = grp; i < ADRT_TR; i += 8) {
+        const int row = row0 + i;
+        if (row >= Hout) break;
+        const int h = h0 + i;
+        T acc = 0;
+        if (h >= -t && h < N) acc += small ? tA[i][c0 - s0] : tA[i][c0 - cA];
+        const int h1 = h + t + b;
+        if (h1 >= -t && h1 < N) acc += small ? tA[h1 - h0][c1 - s0] : tB[h1 - hB][c1 - cB];
+        g[(size_t)row * N + s] = acc;
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) adrt_adj_level_tiled(int n, int m, const T* __restrict__ src,
+                                                            T* __restrict__ dst, size_t S,
+                                                            const int* __restrict__ active) {
+    const int N = 1 << n, w = 1 << (m - 1);
+    const int Hin = N + w - 1, off = 2 * w - 1;  // output rows (level m-1 layout); input row offset (level m)
+    const int col0 = blockIdx.x * 32, row0 = blockIdx.y * ADRT_TR;
+    const size_t slot = blockIdx.z;
+    if (active && !active[slot >> 2]) return;
+    const T* g = src + slot * S;
+    T* o = dst + slot * S;
+    const int h0 = row0 - (w - 1);
+    __shared__ T tg[ADRT_TR + 32][65];
+    const int lane = threadIdx.x & 31, grp = threadIdx.x >> 5;
+    const int Hg = N + 2 * w - 1;
+    auto ld = [&](int h, int c) -> T {
+        const int r = h + off;
+        return (r >= 0 && r < Hg) ? g[(size_t)r * N + c] : (T)0;
+    };
+    const bool small = 2 * w <= 32;
+    const int l = col0 / (2 * w), r0 = col0 - l * 2 * w, half = small ? 0 : r0 / w;
+    const int t0 = small ? 0 : r0 - half * w;
+    int gc0, gh0, ncols;
+    if (small) {
+        gc0 = col0;      // the window's own columns
+        gh0 = h0 - w;    // rows h - t - 1 >= h0 - w
+        ncols = 32;
+    } else {
+        gc0 = l * 2 * w + 2 * t0;                // base columns of t0 .. t0 + 31, and base + 1
+        gh0 = half == 0 ? h0 : h0 - t0 - 32;     // second half reads rows h - t, h - t - 1
+        ncols = 64;
+    }
+    const int nrows = small ? ADRT_TR + w : (half == 0 ? ADRT_TR : ADRT_TR + 32);
+    for (int e = threadIdx.x; e < nrows * ncols; e += 256) {
+        const int r = e / ncols, c = e - r * ncols;
+        tg[r][c] = ld(gh0 + r, gc0 + c);
+    }
+    __syncthreads();
+    const int col = col0 + lane;
+    const int cl = col / (2 * w), r = col - cl * 2 * w, c = r / w, t = r - c * w;
+    const int base = cl * 2 * w + 2 * t - gc0;
+    for (int i = grp; i < ADRT_TR; i += 8) {
+        const int row = row0 + i;
+        if (row >= Hin) break;
+        const int h = h0 + i;
+        T v = 0;
+        if (h >= -t && h < N) {
+            if (c == 0) v = tg[h - gh0][base] + tg[h - gh0][base + 1];
+            else v = tg[h - t - gh0][base] + tg[h - t - 1 - gh0][base + 1];
+        }
+        o[(size_t)row * N + col] = v;
+    }
+}
+
 // level-1 adjoint of the four quadrants, T_q^T and the quadrant sum (adrtcore.py:131-137)
 template <typename T>
 __global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __restrict__ x, size_t S,
@@ -116,8 +232,14 @@ static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, const i
     const T* src = reinterpret_cast<const T*>(x);
     for (int m = 1; m <= n; ++m) {
         T* dst = (m == n) ? reinterpret_cast<T*>(b) : bufs[m & 1];
-        const size_t total = (size_t)(N + (1 << m) - 1) * N * 4 * nimg;
-        adrt_fwd_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
+        const int Hout = N + (1 << m) - 1;
+        const size_t total = (size_t)Hout * N * 4 * nimg;
+        if (m >= 2 && N >= 32 && 4L * nimg <= 65535) {
+            dim3 grid(N / 32, (Hout + ADRT_TR - 1) / ADRT_TR, 4 * nimg);
+            adrt_fwd_level_tiled<T><<<grid, 256, 0, st>>>(n, m, src, dst, S, active);
+        } else {
+            adrt_fwd_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
+        }
         int rc = launch_status("adrt_fwd_level");
         if (rc) return rc;
         src = dst;
@@ -133,8 +255,14 @@ static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, const i
     const T* src = reinterpret_cast<const T*>(b);
     for (int m = n; m >= 2; --m) {
         T* dst = bufs[m & 1];
-        const size_t total = (size_t)(N + (1 << (m - 1)) - 1) * N * 4 * nimg;
-        adrt_adj_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
+        const int Hin = N + (1 << (m - 1)) - 1;
+        const size_t total = (size_t)Hin * N * 4 * nimg;
+        if (N >= 32 && 4L * nimg <= 65535) {
+            dim3 grid(N / 32, (Hin + ADRT_TR - 1) / ADRT_TR, 4 * nimg);
+            adrt_adj_level_tiled<T><<<grid, 256, 0, st>>>(n, m, src, dst, S, active);
+        } else {
+            adrt_adj_level<T><<<grid_of(total), 256, 0, st>>>(n, m, nimg, src, dst, S, active);
+        }
         int rc = launch_status("adrt_adj_level");
         if (rc) return rc;
         src = dst;
