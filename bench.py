@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--serve-rate", type=float, default=2000.0)
     ap.add_argument("--stencil", default=STENCIL, choices=["fp32", "ff", "fp64"],
                     help="precision of the cross-quadrant preconditioner (ff: float-float, about 48 bits)")
+    ap.add_argument("--high-rows", default="dense", choices=["dense", "ff"],
+                    help="large mode: the rows with d_k > dense_cap as dense operators or compensated rows")
     ap.add_argument("--no-extras", action="store_true",
                     help="batch mode: skip the short serve / uneven / large runs appended to the line")
     return ap.parse_args()
@@ -766,14 +768,15 @@ def run_uneven(args):
     print(json.dumps(line), flush=True)
 
 
-def large_result(pkg, dev, steps, warmup, profile_region=False):
+def large_result(pkg, dev, steps, warmup, profile_region=False, high_rows="dense"):
     """N = 2048 (n = 11), hybrid, p = 64, dense_cap 16, FP32 rows with FP64 tables, batch 1 and 8; 40 ellipses plus
-    a 0.1-weighted uniform texture; relative error of the first image against the FP64 pipeline on the same plan."""
+    a 0.1-weighted uniform texture; relative error of the first image against the FP64 pipeline on the same plan.
+    high_rows: the rows with d_k > 16 as dense operators ("dense") or as compensated float-float rows ("ff")."""
     import torch
 
     n = 11
     t0 = time.perf_counter()
-    H = pkg.FastHybridGpu(n, deg_cap=64, dense_cap=DENSE_CAP, precision="fp32", device=dev)
+    H = pkg.FastHybridGpu(n, deg_cap=64, dense_cap=DENSE_CAP, precision="fp32", device=dev, high_rows=high_rows)
     setup_s = time.perf_counter() - t0
     b = _phantom_sinos(pkg, n, 8, 777, dev, REL_SIGMA, ellipses=40, texture=0.1)
     res = {}
@@ -803,6 +806,7 @@ def large_result(pkg, dev, steps, warmup, profile_region=False):
     ref = H.pipeline(1, "fp64").apply(b[:1].contiguous())[0].cpu().numpy()
     H.pipeline(8).tables.raise_if_error()
     return {"results": res, "setup_s": setup_s, "outer_deg": H.outer_deg, "n_dense_freqs": H.eng.n_dense,
+            "high_rows": high_rows, "device_gb": H.pipeline(8).device_bytes() / 1e9,
             "rel_err_vs_fp64": _rel(got, ref), "clocks": clk.summary()}
 
 
@@ -816,7 +820,7 @@ def run_large(args):
     import __graft_entry__ as ge
 
     pkg = ge.load_package()
-    r = large_result(pkg, torch.device("cuda", 0), args.steps, args.warmup, args.profile_region)
+    r = large_result(pkg, torch.device("cuda", 0), args.steps, args.warmup, args.profile_region, args.high_rows)
     line = {"metric": "hybrid-inverse recon/s at N=2048 (batch 8)", "value": r["results"]["batch8"]["recon_s"],
             "unit": "recon/s", "n_gpus": 1, "higher_is_better": True, "dtype": "f32", "data": "synthetic",
             "config": LARGE_CONFIG, **r}
