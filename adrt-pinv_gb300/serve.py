@@ -173,7 +173,9 @@ class SlotLane:
         self.s = 0  # global step counter (the buffer rotation phase is s % 3)
         self.hk = [D] * self.slots  # host mirror of the per-slot iteration counters
         self.req = [None] * self.slots
-        self.stage_in = torch.zeros((1, 4, 2 * N - 1, N), dtype=torch.float64, pin_memory=True)
+        # pinned staging per slot: a slot's staging is written again only at its next admission, after its previous
+        # request's result (and so its input copy) has completed
+        self.stage_in = torch.zeros((self.slots, 4, 2 * N - 1, N), dtype=torch.float64, pin_memory=True)
         self.stage_out = torch.empty((self.slots, N, N), dtype=torch.float64, pin_memory=True)
         self.out_events = []  # (slot, request, event) of result copies in flight
         self.step_events = deque()  # completion events of the steps in flight (at most `depth`)
@@ -231,8 +233,8 @@ class SlotLane:
                 if isinstance(b, torch.Tensor):
                     self.b1[0].copy_(b, non_blocking=b.is_cuda or b.is_pinned())
                 else:
-                    self.stage_in[0].copy_(torch.from_numpy(np.ascontiguousarray(b, dtype=np.float64)))
-                    self.b1.copy_(self.stage_in, non_blocking=True)
+                    self.stage_in[i].copy_(torch.from_numpy(np.ascontiguousarray(b, dtype=np.float64)))
+                    self.b1[0].copy_(self.stage_in[i], non_blocking=True)
                 self.bp.backproject_into(self.b1, self.pipe.y[i:i + 1])
                 cur[i].zero_()
                 prev[i].zero_()
