@@ -520,14 +520,15 @@ class Pipeline:
             bufs += [t.roots64, t.coef64]
         if t._zd is not None:
             bufs.append(t._zd)
-        if getattr(self, "b_in", None) is not None:
-            bufs.append(self.b_in)
+        for name in ("b_in", "b_in2"):
+            if getattr(self, name, None) is not None:
+                bufs.append(getattr(self, name))
         return sum(x.numel() * x.element_size() for x in bufs)
 
     @staticmethod
     def estimate_bytes(plan: Plan, batch, precision="fp32", stencil_precision=None, captured=True):
         """Device bytes a pipeline for (plan, batch, precision) holds once it has run apply (and capture, which adds
-        the input buffer): the buffers of __init__, the two folded dense-row tables (filter of G and of the
+        the two input buffers): the buffers of __init__, the two folded dense-row tables (filter of G and of the
         backprojection) and the dense-row staging, computed without allocating anything."""
         N, L, B = plan.N, plan.L, int(batch)
         rs = PRECISIONS[precision].itemsize
@@ -541,8 +542,8 @@ class Pipeline:
         else:
             total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
         total += L * 2 * rs + 3 * L * 4 + plan.coef.size * rs  # roots; deg and the row lists; coefficients
-        if captured:
-            total += B * 4 * (2 * N - 1) * N * 8
+        if captured:  # the two input buffers of the captured graphs
+            total += 2 * B * 4 * (2 * N - 1) * N * 8
         return int(total)
 
     def capture(self):
@@ -560,7 +561,20 @@ class Pipeline:
             with torch.cuda.graph(self.graph, stream=side):
                 self.x_out = self.apply(self.b_in)
             self.graph_count = self.tables.count - before  # level-rows of one replay
+            # a second graph on a second input buffer: host batches alternate between the two, so that the copy of
+            # the next batch (on its own stream) overlaps the graph of the current one
+            self.b_in2 = torch.zeros_like(self.b_in)
+            self.graph2 = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(self.graph2, stream=side):
+                x2 = self.apply(self.b_in2)
+            self.tables.count -= self.graph_count
+            assert x2.data_ptr() == self.x_out.data_ptr()
         torch.cuda.current_stream(self.device).wait_stream(side)
+        self.copy_stream = torch.cuda.Stream(device=self.device)
+        self._flip = 0
+        self._free = [None, None]  # per input buffer: the event after the graph that last read it
+        self._err_host = torch.zeros(1, dtype=torch.int32, pin_memory=True)
+        self._err_event = None  # the previous host-side replay's error-flag copy
         return self
 
     def replay(self, b=None):
@@ -571,6 +585,48 @@ class Pipeline:
         self.graph.replay()
         self.tables.count += self.graph_count
         return self.x_out
+
+    def replay_host(self, b, out):
+        """Host batch in, host result out, pipelined across calls: b is copied into one of the two input buffers on
+        the copy stream (waiting only for the graph that last read that buffer), the matching graph replays on the
+        current stream once the copy is done, and the result and the dense kernel's error flag are copied back
+        without a host synchronisation. The error flag of the PREVIOUS host replay is checked here, after the
+        copy is queued (so that copy still overlaps the previous graph); check_host() checks the last one."""
+        i = self._flip
+        self._flip ^= 1
+        buf, graph = (self.b_in, self.graph) if i == 0 else (self.b_in2, self.graph2)
+        cur = torch.cuda.current_stream(self.device)
+        cs = self.copy_stream
+        if self._free[i] is not None:
+            cs.wait_event(self._free[i])
+        with torch.cuda.stream(cs):
+            buf.copy_(b, non_blocking=True)
+        copied = torch.cuda.Event()
+        copied.record(cs)
+        self.check_host()
+        cur.wait_event(copied)
+        graph.replay()
+        self.tables.count += self.graph_count
+        free = torch.cuda.Event()
+        free.record(cur)
+        self._free[i] = free
+        out.copy_(self.x_out, non_blocking=True)
+        self._err_host.copy_(self.tables.err, non_blocking=True)
+        self.tables.err.zero_()
+        self._err_event = torch.cuda.Event()
+        self._err_event.record(cur)
+        return out
+
+    def check_host(self):
+        """Raise if the last replay_host's dense-row launch gave up on a bounded wait (waits for that replay)."""
+        ev, self._err_event = getattr(self, "_err_event", None), None
+        if ev is None:
+            return
+        ev.synchronize()
+        code = int(self._err_host.item())
+        if code:
+            raise RuntimeError("dense_tc_kernel: an mbarrier wait ran out; the dense-row results of the previous "
+                               "batch were not written" + ("" if code == 1 else " (and the MMA drain ran out)"))
 
     def first_step(self, y, x_out, a):
         """x_1 = a P(y) (P = identity for L_p): the outer iteration's first step (fastops.py:250)."""

@@ -215,6 +215,13 @@ class _GpuInverse:
             pipe.capture()  # the second call of this batch size records the whole apply as a CUDA graph
             before = pipe.tables.count
         if self.graphs and getattr(pipe, "graph", None) is not None:
+            if out is not None and host_in and not out.is_cuda and bt.dtype == torch.float64 and bt.is_pinned():
+                # host in, host out: pipelined across calls (the copy of this batch overlaps the previous graph);
+                # the dense kernel's error flag of a call is checked at the next call or by check()
+                pipe.replay_host(bt.contiguous(), out[None] if single else out)
+                self._count(pipe, before)
+                self._last_pipe = pipe
+                return out
             x = pipe.replay(bt.contiguous())
         else:
             x = pipe.apply(bt.to(self.device, non_blocking=True).contiguous())
@@ -235,6 +242,17 @@ class _GpuInverse:
             pipe.tables.raise_if_error()
             return res
         return x.clone()
+
+
+def _check(self):
+    """Wait for the last pipelined host call (apply with pinned host input and a host `out`) and raise if its dense
+    rows failed."""
+    pipe = getattr(self, "_last_pipe", None)
+    if pipe is not None:
+        pipe.check_host()
+
+
+_GpuInverse.check = _check
 
 
 class FastLpGpu(_GpuInverse):

@@ -164,7 +164,7 @@ def test_pipeline_estimate_matches_buffers(pkg):
     expect = B * 2 * L * N * 8 + 3 * B * N * N * 4 + 4 * B * N * N * 8 + 4 * B * N * N * 4
     expect += 2 * nd * N * N * 8 + nd * B * N * 8 + L * 8 + 3 * L * 4 + plan.coef.size * 4
     assert est == expect
-    assert Pipeline.estimate_bytes(plan, 3, "fp32") - est == B * 4 * (2 * N - 1) * N * 8
+    assert Pipeline.estimate_bytes(plan, 3, "fp32") - est == 2 * B * 4 * (2 * N - 1) * N * 8
 
 
 def test_slot_level_admission_between_steps(pkg):
