@@ -2,19 +2,23 @@
 
 Workload (one step): the hybrid explicit inverse (fastops.FastHybrid.apply semantics) of a batch of 64 noisy
 sinograms of seeded 10-ellipse phantoms at N = 256 (n = 8), inner degrees capped at p = 32, dense low-frequency
-table for d_k > 16, FP32 row engine / FFTs / stencil with FP64 tables and FP64 outer iteration. Metric: whole-job
-reconstructions per second. Every step's inputs (268 MB of FP64 sinograms) exceed the 129 MB L2, so no flush is
-needed between steps.
+table for d_k > 16, FP32 row engine / FFTs and cross-quadrant preconditioner (--stencil ff|fp64 for the FP64-class
+forms) with FP64 tables and FP64 outer iteration. Metric: whole-job reconstructions per second. Every step's inputs
+(268 MB of FP64 sinograms) exceed the 129 MB L2, so no flush is needed between steps.
 
   value : device-resident sinograms, K timed steps of Pipeline.apply (CUDA events, barrier + sync both sides).
-  e2e   : the public API FastHybridGpu.apply on pinned host sinograms with the result read back to pinned host
-          memory every step (H2D + D2H inside the timed region).
+  e2e   : the public API FastHybridGpu.apply on pinned host sinograms into a pinned host result every step (H2D + D2H
+          inside the timed region; consecutive calls overlap a batch's copy with the previous batch's graph).
   roofline : the row engine (rows_prog_kernel), the dominant kernel, timed live with CUDA events on its stream;
           algorithmic FLOPs = level-rows x 8N (the reference's cost unit, fastops.py:166); peak = FP32 FMA
           throughput measured in this run by the library's probe kernel.
   cpu_baseline : the reference's C++-engine path (FastHybridCpp semantics: C row kernels + NumPy) timed on this
           host's cores on one image of the same workload, same plan.
-`--impl reference` times only that CPU path (rank 0) on the same config and prints its own line.
+  extras (one-GPU runs, --no-extras to skip): preconditioner_ff / _fp32 (the other preconditioner precision),
+          adrt_int32, cgls, serve (p50/p99 at a sustainable rate and at 2000 req/s), uneven (stream-per-class graph
+          and persistent rows), large (N=2048, batch 1 and 8).
+`--impl reference` times only that CPU path (rank 0) on the same config and prints its own line; --mode
+serve|uneven|large runs one of the other workloads alone.
 """
 
 import argparse
