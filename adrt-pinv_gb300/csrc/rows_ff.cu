@@ -18,7 +18,7 @@
 
 namespace adrt {
 
-constexpr int FF_THREADS = 256;
+constexpr int FF_THREADS = 512;  // the largest CTA; N <= 512 rows take 256 threads
 
 // forward levels lo..hi: o[2t] = f0[t] + z^t f1[t], o[2t+1] = f0[t] + z^(t+1) f1[t]
 __device__ void ff_fwd(ffc*& a, ffc*& b, int N, int lo, int hi, const ffc* tw) {
@@ -151,7 +151,8 @@ int rows_ff_run(const adrt_row_job* J, cudaStream_t st) {
     if (per_sm > 8) per_sm = 8;
     long grid = (long)device_sm_count() * per_sm;
     if (grid > total_l) grid = total_l;
-    rows_ff_kernel<<<(int)grid, FF_THREADS, smem, st>>>(*J, (int)total_l);
+    const int threads = N >= 1024 ? FF_THREADS : 256;  // at least two butterflies per thread and level
+    rows_ff_kernel<<<(int)grid, threads, smem, st>>>(*J, (int)total_l);
     return launch_status("rows_ff_kernel");
 }
 
