@@ -14,7 +14,8 @@ lanes of different sizes run concurrently on the GPU. Two kinds of lane:
     flight has finished.
 
 A lane for a new size is created only if its device memory (estimated before anything is allocated) fits the HBM
-budget beside the lanes that exist; idle lanes with no waiting requests are evicted, least recently used first, to
+budget beside the lanes that exist and the memory the device can still give (the driver's free memory plus what the
+caching allocator holds unused); idle lanes with no waiting requests are evicted, least recently used first, to
 make room, and otherwise the new size waits. A request's state (sinogram, packed rows, iterates) stays on the device
 for its whole inverse.
 
@@ -322,9 +323,17 @@ class InverseServer:
         self.clock = time.perf_counter
         self.evictions = 0
         self.max_busy = 0  # most lanes seen with a batch in flight at once
+        self.device_free = self._device_free  # bytes the device can still give (replaceable for host tests)
 
     def memory_in_use(self):
         return sum(l.device_bytes() for l in self.lanes.values())
+
+    def _device_free(self):
+        """Free device memory as the driver reports it plus what torch's caching allocator holds unused."""
+        if self.device.type != "cuda":
+            return float("inf")
+        free, _ = torch.cuda.mem_get_info(self.device)
+        return free + torch.cuda.memory_reserved(self.device) - torch.cuda.memory_allocated(self.device)
 
     def _admit_lane(self, n):
         """The lane of size n, created if the budget allows (evicting idle lanes without waiting requests); None
@@ -339,11 +348,18 @@ class InverseServer:
             raise MemoryError(f"a lane for n={n} needs {need} bytes, above the budget of {self.budget:.0f}")
         victims = sorted((self.last_used.get(m, 0.0), m) for m, l in self.lanes.items()
                          if not l.in_flight() and not self.queues.get(m))
-        while self.memory_in_use() + need > self.budget and victims:
+        # admission by the HBM budget and by what the device can actually still give (other users of the GPU,
+        # other allocations of this process)
+        def fits():
+            return self.memory_in_use() + need <= self.budget and need <= self.device_free()
+
+        while not fits() and victims:
             _, m = victims.pop(0)
             self.lanes.pop(m).release()
             self.evictions += 1
-        if self.memory_in_use() + need > self.budget:
+            if self.device.type == "cuda":
+                torch.cuda.empty_cache()
+        if not fits():
             return None
         self.lanes[n] = self.lane_cls(inv, self.slots(n), self.device)
         return self.lanes[n]

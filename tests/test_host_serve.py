@@ -188,3 +188,17 @@ def test_slot_level_admission_between_steps(pkg):
         pass
     assert {r.rid for r in S.finished} == {0, 1, 2}
     assert lane.steps == 6  # a: steps 1-3, b: 2-4, c: 4-6, overlapping
+
+
+def test_admission_by_device_free_memory(pkg):
+    """A lane that fits the budget but not the memory the device can still give waits (the queue keeps its
+    requests) until memory frees up."""
+    S, serve = _server(pkg, budget=1e12)
+    free = {"bytes": 100}  # far less than one lane (4 slots x 64 x 64)
+    S.device_free = lambda: free["bytes"]
+    S.submit(serve.Request(0, 6, None))
+    assert S.step() == 1 and not S.lanes
+    free["bytes"] = 1e9
+    while S.step():
+        pass
+    assert len(S.finished) == 1 and 6 in S.lanes
