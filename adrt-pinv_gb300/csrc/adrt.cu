@@ -202,6 +202,109 @@ __global__ void __launch_bounds__(256) adrt_adj_level_tiled(int n, int m, const 
     }
 }
 
+// ------------------------------------------------------------------ the first four levels in shared memory
+// Levels 1..4 only combine columns within blocks of 16 (level m pairs the halves of blocks of 2^m columns), so a CTA
+// can take one 16-column block of one quadrant through all four levels in shared memory: the forward pass reads the
+// T_q strip once and writes level 4; the adjoint reads level 4 and writes level 1 (the quadrant sum stays with
+// adrt_adj_final). Rows in shared memory have a stride of 17 elements (conflict-free column walks).
+constexpr int F4_SP = 17;
+
+template <typename T> static size_t f4_smem(int N) { return 2 * (size_t)(N + 15) * F4_SP * sizeof(T); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) adrt_fwd_levels14(int n, const T* __restrict__ x, T* __restrict__ dst, size_t S,
+                                                         const int* __restrict__ active) {
+    const int N = 1 << n;
+    const int c0 = blockIdx.x * 16, q = blockIdx.y, img = blockIdx.z;
+    if (active && !active[img]) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* a = reinterpret_cast<T*>(smem_raw);
+    T* b = a + (size_t)(N + 15) * F4_SP;
+    const T* xi = x + (size_t)img * N * N;
+    // level 0: the T_q strip (rows h = 0..N-1); quadrants 0 and 3 read image rows, so there consecutive threads take
+    // consecutive h, the others consecutive columns
+    for (int e = threadIdx.x; e < N * 16; e += 256) {
+        int h, c;
+        if (q == 1 || q == 2) {
+            h = e >> 4;
+            c = e & 15;
+        } else {
+            c = e >> n;
+            h = e & (N - 1);
+        }
+        a[h * F4_SP + c] = tq_read(xi, N, q, h, c0 + c);
+    }
+    __syncthreads();
+    int off = 0;  // row offset of the level held in a (level m-1 data: 2^(m-1) - 1)
+    for (int m = 1; m <= 4; ++m) {
+        const int w = 1 << (m - 1), Hout = N + 2 * w - 1;
+        for (int e = threadIdx.x; e < Hout * 16; e += 256) {
+            const int row = e >> 4, cc = e & 15;
+            const int h = row - (2 * w - 1);
+            const int l = cc / (2 * w), rr = cc - l * 2 * w, t = rr >> 1, bb = rr & 1;
+            const int ca = l * 2 * w + t, cb = ca + w;
+            T acc = 0;
+            if (h >= -t && h < N) acc += a[(h + off) * F4_SP + ca];
+            const int h1 = h + t + bb;
+            if (h1 >= -t && h1 < N) acc += a[(h1 + off) * F4_SP + cb];
+            b[row * F4_SP + cc] = acc;
+        }
+        __syncthreads();
+        T* tmp = a;
+        a = b;
+        b = tmp;
+        off = 2 * w - 1;
+    }
+    T* g = dst + ((size_t)img * 4 + q) * S;
+    for (int e = threadIdx.x; e < (N + 15) * 16; e += 256) {
+        const int row = e >> 4, cc = e & 15;
+        g[(size_t)row * N + c0 + cc] = a[row * F4_SP + cc];
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) adrt_adj_levels42(int n, const T* __restrict__ src, T* __restrict__ dst,
+                                                         size_t S, const int* __restrict__ active) {
+    const int N = 1 << n;
+    const int c0 = blockIdx.x * 16;
+    const size_t slot = blockIdx.y;
+    if (active && !active[slot >> 2]) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* a = reinterpret_cast<T*>(smem_raw);
+    T* b = a + (size_t)(N + 15) * F4_SP;
+    const T* g = src + slot * S;
+    for (int e = threadIdx.x; e < (N + 15) * 16; e += 256) {
+        const int row = e >> 4, cc = e & 15;
+        a[row * F4_SP + cc] = g[(size_t)row * N + c0 + cc];
+    }
+    __syncthreads();
+    for (int m = 4; m >= 2; --m) {
+        // level-m data in a (rows h + 2w - 1) -> level m-1 data in b (rows h + w - 1), as adj_at
+        const int w = 1 << (m - 1), Hin = N + w - 1, goff = 2 * w - 1;
+        for (int e = threadIdx.x; e < Hin * 16; e += 256) {
+            const int row = e >> 4, col = e & 15;
+            const int h = row - (w - 1);
+            const int l = col / (2 * w), r = col - l * 2 * w, c = r / w, t = r - c * w;
+            T v = 0;
+            if (h >= -t && h < N) {
+                const int base = l * 2 * w + 2 * t;
+                if (c == 0) v = a[(h + goff) * F4_SP + base] + a[(h + goff) * F4_SP + base + 1];
+                else v = a[(h - t + goff) * F4_SP + base] + a[(h - t - 1 + goff) * F4_SP + base + 1];
+            }
+            b[row * F4_SP + col] = v;
+        }
+        __syncthreads();
+        T* tmp = a;
+        a = b;
+        b = tmp;
+    }
+    T* o = dst + slot * S;
+    for (int e = threadIdx.x; e < (N + 1) * 16; e += 256) {  // level 1: N + 1 rows
+        const int row = e >> 4, cc = e & 15;
+        o[(size_t)row * N + c0 + cc] = a[row * F4_SP + cc];
+    }
+}
+
 // level-1 adjoint of the four quadrants, T_q^T and the quadrant sum (adrtcore.py:131-137)
 template <typename T>
 __global__ void adrt_adj_final(int n, int nimg, const T* __restrict__ src, T* __restrict__ x, size_t S,
@@ -230,7 +333,18 @@ static int fwd_t(int n, int nimg, const void* x, void* b, void* scratch, const i
     const size_t S = (size_t)(2 * N - 1) * N;
     T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
     const T* src = reinterpret_cast<const T*>(x);
-    for (int m = 1; m <= n; ++m) {
+    int m0 = 1;
+    if (n >= 4 && f4_smem<T>(N) <= 200 * 1024 && nimg <= 65535) {
+        // levels 1..4 in one pass per 16-column block and quadrant
+        T* dst = (n == 4) ? reinterpret_cast<T*>(b) : bufs[0];
+        const size_t smem = f4_smem<T>(N);
+        if (int rc = ensure_smem((const void*)adrt_fwd_levels14<T>, smem)) return rc;
+        adrt_fwd_levels14<T><<<dim3(N / 16, 4, nimg), 256, smem, st>>>(n, src, dst, S, active);
+        if (int rc = launch_status("adrt_fwd_levels14")) return rc;
+        src = dst;
+        m0 = 5;
+    }
+    for (int m = m0; m <= n; ++m) {
         T* dst = (m == n) ? reinterpret_cast<T*>(b) : bufs[m & 1];
         const int Hout = N + (1 << m) - 1;
         const size_t total = (size_t)Hout * N * 4 * nimg;
@@ -253,7 +367,8 @@ static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, const i
     const size_t S = (size_t)(2 * N - 1) * N;
     T* bufs[2] = {reinterpret_cast<T*>(scratch), reinterpret_cast<T*>(scratch) + S * 4 * nimg};
     const T* src = reinterpret_cast<const T*>(b);
-    for (int m = n; m >= 2; --m) {
+    const bool fuse = n >= 4 && f4_smem<T>(N) <= 200 * 1024 && 4L * nimg <= 65535;
+    for (int m = n; m >= (fuse ? 5 : 2); --m) {
         T* dst = bufs[m & 1];
         const int Hin = N + (1 << (m - 1)) - 1;
         const size_t total = (size_t)Hin * N * 4 * nimg;
@@ -265,6 +380,15 @@ static int adj_t(int n, int nimg, const void* b, void* x, void* scratch, const i
         }
         int rc = launch_status("adrt_adj_level");
         if (rc) return rc;
+        src = dst;
+    }
+    if (fuse) {
+        // levels 4..2 in one pass per 16-column block and quadrant: level 4 in, level 1 out
+        T* dst = (src == bufs[0]) ? bufs[1] : bufs[0];
+        const size_t smem = f4_smem<T>(N);
+        if (int rc = ensure_smem((const void*)adrt_adj_levels42<T>, smem)) return rc;
+        adrt_adj_levels42<T><<<dim3(N / 16, 4 * nimg), 256, smem, st>>>(n, src, dst, S, active);
+        if (int rc = launch_status("adrt_adj_levels42")) return rc;
         src = dst;
     }
     adrt_adj_final<T><<<grid_of((size_t)N * N * nimg), 256, 0, st>>>(n, nimg, src, reinterpret_cast<T*>(x), S, active);
