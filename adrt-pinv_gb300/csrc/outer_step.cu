@@ -8,6 +8,7 @@
 // from the neighbouring CTAs' shared memory (distributed shared memory) after a cluster barrier per step.
 // Pair rows (2i, 2i+1) never straddle a band (BAND is even), so the i^1 neighbour is always local.
 #include <cooperative_groups.h>
+#include <type_traits>
 
 #include "common.cuh"
 #include "ff.cuh"
@@ -84,11 +85,21 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     const TP* p1 = reinterpret_cast<const TP*>(A.p1);
     const TP* p2 = reinterpret_cast<const TP*>(A.p2);
 
-    // residual into shared memory (the partial images summed in their own precision, the difference in FP64)
-    for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+    // residual into shared memory (the partial images summed in their own precision, the difference in FP64); two
+    // neighbouring elements per thread and load (E and the image offsets are even)
+    using TP2 = typename std::conditional<sizeof(TP) == 4, float2, double2>::type;
+    for (int e = 2 * threadIdx.x; e < E; e += 2 * OS_THREADS) {
         const size_t g = base + e;
-        const TP t = p0 ? (p0[g] + p1[g]) + p2[g] : (TP)0;
-        s[e] = Ar::from_d(A.y[g] - (double)t);
+        TP t0 = (TP)0, t1 = (TP)0;
+        if (p0) {
+            const TP2 a = *reinterpret_cast<const TP2*>(p0 + g), b = *reinterpret_cast<const TP2*>(p1 + g),
+                      c = *reinterpret_cast<const TP2*>(p2 + g);
+            t0 = (a.x + b.x) + c.x;
+            t1 = (a.y + b.y) + c.y;
+        }
+        const double2 yv = *reinterpret_cast<const double2*>(A.y + g);
+        s[e] = Ar::from_d(yv.x - (double)t0);
+        s[e + 1] = Ar::from_d(yv.y - (double)t1);
     }
     __syncthreads();
 
@@ -174,16 +185,18 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     // outer update in FP64
     const double oa = A.om_img ? A.om_img[2 * img] : A.om_a;
     const double o1 = A.om_img ? A.om_img[2 * img + 1] : A.om_1;
-    for (int e = threadIdx.x; e < E; e += OS_THREADS) {
+    for (int e = 2 * threadIdx.x; e < E; e += 2 * OS_THREADS) {
         const size_t g = base + e;
-        const double rv = Ar::to_d(r[e]);
+        const double r0 = Ar::to_d(r[e]), r1 = Ar::to_d(r[e + 1]);
+        double2 out;
         if (!A.x) {
-            A.xn[g] = A.a0 * rv;
+            out = make_double2(A.a0 * r0, A.a0 * r1);
         } else {
-            const double xv = A.x[g];
-            const double prev = A.xp ? A.xp[g] : 0.0;
-            A.xn[g] = xv + oa * rv + o1 * (xv - prev);
+            const double2 xv = *reinterpret_cast<const double2*>(A.x + g);
+            const double2 pv = A.xp ? *reinterpret_cast<const double2*>(A.xp + g) : make_double2(0.0, 0.0);
+            out = make_double2(xv.x + oa * r0 + o1 * (xv.x - pv.x), xv.y + oa * r1 + o1 * (xv.y - pv.y));
         }
+        *reinterpret_cast<double2*>(A.xn + g) = out;
     }
 }
 
