@@ -11,6 +11,8 @@
 // unpack: both pairs of a column block are transformed back (1/L), only the first N offsets are kept, and the
 //         four quadrant strips are scattered with TqT and cropped into three image-space partial sums:
 //         colpart (quadrants II+III: out columns), rowpart0 (quadrant I: out rows), rowpart3 (quadrant IV).
+#include <type_traits>
+
 #include "common.cuh"
 #include "launch.h"
 
@@ -109,7 +111,65 @@ __global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<rea
 
     // ---- gather the packed strips of columns c0..c0+CB-1 into tile[i][c]; every thread issues its E loads before
     // its shared-memory stores (E independent loads in flight)
-    if (src_kind == 0) {
+    if (src_kind == 0 && CB % 2 == 0) {
+        // two neighbouring elements per load: column pairs of the column reads, offset pairs of the row reads
+        using S2 = typename std::conditional<sizeof(SRC) == 8, double2, float2>::type;
+        constexpr int HC = CB / 2, HE = F::E / 2, HL = L / 2;
+        const size_t ib = (size_t)img * N * N;
+        // column reads: pair 0 imag = x[N-1-i, c] (quadrant II), pair 1 real = x[i, c] (quadrant III)
+        real va[HE], vb[HE];
+#pragma unroll
+        for (int k = 0; k < HE; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int c = 2 * (e % HC), i = e / HC;
+            va[k] = 0;
+            vb[k] = 0;
+            if (i < N) {
+                const S2 w = *reinterpret_cast<const S2*>(src + ib + (size_t)(pair == 0 ? N - 1 - i : i) * N + c0 + c);
+                va[k] = (real)w.x;
+                vb[k] = (real)w.y;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < HE; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int c = 2 * (e % HC), i = e / HC;
+            if (pair == 0) {
+                tile[i * CP + c].y = va[k];
+                tile[i * CP + c + 1].y = vb[k];
+            } else {
+                tile[i * CP + c].x = va[k];
+                tile[i * CP + c + 1].x = vb[k];
+            }
+        }
+        // row reads: pair 0 real = x[c, N-1-i] (quadrant I), pair 1 imag = x[N-1-c, N-1-i] (quadrant IV); the pair
+        // (i, i+1) is the element pair (N-2-i, N-1-i) of the image row
+#pragma unroll
+        for (int k = 0; k < HE; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int i = 2 * (e % HL), c = e / HL;
+            va[k] = 0;
+            vb[k] = 0;
+            if (i < N) {
+                const int rowx = (pair == 0) ? (c0 + c) : (N - 1 - c0 - c);
+                const S2 w = *reinterpret_cast<const S2*>(src + ib + (size_t)rowx * N + (N - 2 - i));
+                va[k] = (real)w.y;  // offset i
+                vb[k] = (real)w.x;  // offset i + 1
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < HE; ++k) {
+            const int e = threadIdx.x + k * nthr;
+            const int i = 2 * (e % HL), c = e / HL;
+            if (pair == 0) {
+                tile[i * CP + c].x = va[k];
+                tile[(i + 1) * CP + c].x = vb[k];
+            } else {
+                tile[i * CP + c].y = va[k];
+                tile[(i + 1) * CP + c].y = vb[k];
+            }
+        }
+    } else if (src_kind == 0) {
         const size_t ib = (size_t)img * N * N;
         // column reads: pair 0 imag = x[N-1-i, c] (quadrant II), pair 1 real = x[i, c] (quadrant III)
         real v[F::E];
