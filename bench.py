@@ -18,7 +18,7 @@ forms) with FP64 tables and FP64 outer iteration. Metric: whole-job reconstructi
           adrt_int32, cgls, serve (p50/p99 at a sustainable rate and at 2000 req/s), uneven (stream-per-class graph
           and persistent rows), large (N=2048, batch 1 and 8).
 `--impl reference` times only that CPU path (rank 0) on the same config and prints its own line; --mode
-serve|uneven|large runs one of the other workloads alone.
+serve|uneven|large|adrt runs one of the other workloads alone.
 """
 
 import argparse
@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--n", type=int, default=N_LOG2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile-region", action="store_true", help="cudaProfilerStart/Stop around the timed steps")
-    ap.add_argument("--mode", default="batch", choices=["batch", "serve", "uneven", "large"],
+    ap.add_argument("--mode", default="batch", choices=["batch", "serve", "uneven", "large", "adrt"],
                     help="batch: the headline N=256 batch-64 workload; serve: Poisson mixed-N request loop; "
                          "uneven: 512 mixed N/p/method sinograms in one CUDA graph; large: N=2048, batch 1 and 8")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
@@ -832,6 +832,19 @@ def run_large(args):
     print(json.dumps(line), flush=True)
 
 
+def run_adrt(args):
+    """The spatial ADRT (int32, forward and transpose) and CGLS iterations alone: their HBM rates."""
+    import torch
+
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    line = {"metric": "spatial ADRT int32 images/s and CGLS image-iterations/s at N=256", "n_gpus": 1,
+            "adrt_int32": adrt_int32_timing(pkg, args.n, args.batch, args.steps, torch),
+            "cgls": cgls_timing(pkg, args.n, 16, 50, torch)}
+    print(json.dumps(line), flush=True)
+
+
 if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
@@ -842,5 +855,7 @@ if __name__ == "__main__":
         run_uneven(a)
     elif a.mode == "large":
         run_large(a)
+    elif a.mode == "adrt":
+        run_adrt(a)
     else:
         run_ours(a)
