@@ -11,6 +11,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libadrt_pinv_gb300.so")
 
 F32, F64, I32, I64, F32X2 = 0, 1, 2, 3, 4
+OS_SHARED = 0x100  # band flag of adrt_outer_step: the shared-memory form
 OP_B, OP_BT, OP_M, OP_P = 0, 1, 2, 3
 MAX_OPS = 8
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory", 4: "unsupported"}

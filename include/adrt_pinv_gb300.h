@@ -175,12 +175,14 @@ int adrt_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const 
  *   1: g1_inv with g1_deg steps, 2: lorr_inv);  x_new = x + om_a r + om_1 (x - x_prev)  (x == NULL: x_new = a0 r;
  *   x_prev NULL: 0).
  * y, x, x_prev, x_new are FP64; s and the stencil iterates are dtype (F32, F64 or F32X2, float-float on the FP32
- * pipe). One thread-block cluster per image keeps the
- * image in shared memory for every stencil step. g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
+ * pipe). One thread-block cluster per image keeps the image on chip for every stencil step: in registers (FP32
+ * stencil and parts, 64 <= N <= 512) or in shared memory (the other types and sizes, or band | ADRT_OS_SHARED).
+ * g1_coef is a HOST array: a, then (omega_k a, omega_k - 1) for
  * k = 1..g1_deg-1 (cheb_solve, fasthybrid.py:114-126). om_img (nullable, DEVICE, with x given): per-image pairs
  * (om_a, om_1) that replace om_a and om_1, so that images at different outer iterations step together (slot-level
  * serving). band: rows of an image per CTA, 16 or 32 (0: chosen from the batch). Supported:
  * n <= adrt_outer_step_max_n(dtype). */
+#define ADRT_OS_SHARED 0x100 /* band flag: the shared-memory form of the fused outer step */
 int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, const void* p0, const void* p1,
                     const void* p2, const double* x, const double* x_prev, double* x_new, double om_a, double om_1,
                     double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, int band,

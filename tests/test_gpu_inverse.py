@@ -191,6 +191,46 @@ def test_fused_outer_step_matches_separate_kernels(pkg, prec, n, precond, nimg):
     assert (out_f - out_s).abs().max().item() / out_s.abs().max().item() < tol
 
 
+@pytest.mark.parametrize("precond", ["g1", "lorr", "none"])
+@pytest.mark.parametrize("n,nimg,band", [(6, 3, 0), (7, 5, 16), (8, 3, 0), (8, 40, 0), (8, 40, 16), (9, 3, 32),
+                                         (9, 2, 16)])
+def test_register_outer_step_matches_shared_form(pkg, n, nimg, band, precond):
+    """The register-resident fused outer step (FP32 stencil and partial images, 64 <= N <= 512: iterates in
+    registers, column neighbours by warp shuffle, halo rows and warp-edge columns through shared memory) against the
+    shared-memory form (ADRT_OS_SHARED) on the same inputs, with per-image outer coefficients: the same arithmetic
+    term for term, so equal up to FP32 contraction differences (1e-6). The G_1 preconditioner alone against the
+    oracle's g1_inv (fasthybrid.py:114-130) at FP32 accuracy (1e-5)."""
+    import torch
+
+    N = 1 << n
+    method = "lp" if precond == "none" else "hybrid"
+    plan = pkg.Plan(method, n, np.full(2 * N, 4.0), precond="g1" if precond == "none" else precond, outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, nimg, "fp32")
+    assert pipe.fused_outer_ok()
+    g = torch.Generator(device="cuda").manual_seed(n + band)
+    y = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    pipe.parts.normal_(generator=g)
+    x = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    xp = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    om = torch.rand((nimg, 2), dtype=torch.float64, device="cuda", generator=g)
+    outs = []
+    for shared in (False, True):
+        pipe.band = band | (pkg._lib.OS_SHARED if shared else 0)
+        o1 = torch.empty_like(x)
+        o2 = torch.empty_like(x)
+        pipe.fused_outer_step(y, True, x, xp, o1, 0.0, 0.0, 0.0, om_img=om)
+        pipe.fused_outer_step(y, False, None, None, o2, 0.0, 0.0, 0.5)
+        outs.append((o1, o2))
+    pipe.band = 0
+    for a, b in zip(*outs):
+        assert (a - b).abs().max().item() / b.abs().max().item() < 1e-6
+    if precond == "g1":
+        got = outs[0][1].cpu().numpy()
+        yh = y.cpu().numpy()
+        for i in range(min(nimg, 3)):
+            assert rel_err(got[i], 0.5 * O.g1_inv(yh[i])) < 1e-5
+
+
 @pytest.mark.parametrize("sprec,tol", [("fp64", 1e-12), ("ff", 1e-10)])
 @pytest.mark.parametrize("n,nimg", [(4, 2), (6, 3), (8, 3), (8, 40)])
 def test_fused_cross_quadrant_inverse_high_precision(pkg, sprec, tol, n, nimg):
