@@ -65,6 +65,7 @@ class PcgState(ctypes.Structure):
 _P = ctypes.c_void_p
 _I = ctypes.c_int
 _D = ctypes.c_double
+_L = ctypes.c_longlong
 PROTOTYPES = {
     "bfly_rows": [_I, _I, _P, _P, _I, _I, _I, _I],
     "cheb_rows": [_I, _I, _P, _P, _P, _P, _D, _P, _P, _I, _I, _I, _P],
@@ -82,7 +83,7 @@ PROTOTYPES = {
     "adrt_twiddle_table": [_I, _I, _I, _P, _P, _P],
     "adrt_power_rows": [_I, _I, _I, _P, _P, _I, _I, _D, _P, _P, _P],
     "adrt_cert_rowsum_dev": [_I, _I, _P, _I, _P, _P],
-    "adrt_pack_fft": [_I, _I, _I, _I, _I, _P, _P, _P, _I, _P],
+    "adrt_pack_fft": [_I, _I, _I, _I, _I, _P, _L, _P, _P, _I, _P],
     "adrt_ifft_unpack": [_I, _I, _I, _P, _P, _P, _P, _P, _I, _P],
     "adrt_resid": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P],
     "adrt_g1_step": [_I, _I, _I, _P, _P, _P, _P, _D, _D, _D, _P],
@@ -91,6 +92,8 @@ PROTOTYPES = {
     "adrt_sum3": [_I, _I, _I, _P, _P, _P, _P, _I, _P],
     "adrt_outer_step": [_I, _I, _I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _I, _P],
     "adrt_outer_step_max_n": [_I],
+    "adrt_outer_step_ff": [_I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _I, _P],
+    "adrt_ff_to_f64": [_I, _I, _P, _P, _P],
     "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _I, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_transpose": [_I, _I, _I, _P, _P, _P, _P],

@@ -237,9 +237,9 @@ int adrt_cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* ou
     return cert_rowsum_dev(n, K, omega, m_lo, out, as_stream(stream));
 }
 
-int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-                  int cols, void* stream) {
-    return pack_fft(dtype, n, nimg, src_kind, src_dtype, src, Y, roots, cols, as_stream(stream));
+int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, long long src_stride,
+                  void* Y, const void* roots, int cols, void* stream) {
+    return pack_fft(dtype, n, nimg, src_kind, src_dtype, src, src_stride, Y, roots, cols, as_stream(stream));
 }
 
 int adrt_ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* rowpart0, void* rowpart3,
@@ -280,6 +280,17 @@ int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y
 }
 
 int adrt_outer_step_max_n(int dtype) { return outer_step_max_n(dtype); }
+
+int adrt_outer_step_ff(int n, int nimg, const float* y, const float* p0, const float* p1, const float* p2,
+                       const float* x, const float* x_prev, float* x_new, double om_a, double om_1, double a0,
+                       int precond, int g1_deg, const double* g1_coef, const double* om_img, int band, void* stream) {
+    return outer_step_ff(n, nimg, y, p0, p1, p2, x, x_prev, x_new, om_a, om_1, a0, precond, g1_deg, g1_coef, om_img,
+                         band, as_stream(stream));
+}
+
+int adrt_ff_to_f64(int n, int nimg, const float* x, double* out, void* stream) {
+    return ff_to_f64(n, nimg, x, out, as_stream(stream));
+}
 
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
                     long long img_stride, void* Zd, int32_t* err, int use_tc, int tile, void* stream) {

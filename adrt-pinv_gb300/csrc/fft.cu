@@ -94,7 +94,7 @@ template <typename real, int l, int CB> struct FftLaunch {
 
 template <typename real, int l, int CB, typename SRC>
 __global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<real, l, CB>::pack_min)
-    pack_fft_kernel(int nimg, int src_kind, const SRC* __restrict__ src, cplx<real>* __restrict__ Y,
+    pack_fft_kernel(int nimg, int src_kind, const SRC* __restrict__ src, long long src_stride, cplx<real>* __restrict__ Y,
                     const cplx<real>* __restrict__ roots_g) {
     using F = FftCfg<l>;
     using C = cplx<real>;
@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<rea
         // two neighbouring elements per load: column pairs of the column reads, offset pairs of the row reads
         using S2 = typename std::conditional<sizeof(SRC) == 8, double2, float2>::type;
         constexpr int HC = CB / 2, HE = F::E / 2, HL = L / 2;
-        const size_t ib = (size_t)img * N * N;
+        const size_t ib = (size_t)img * src_stride;
         // column reads: pair 0 imag = x[N-1-i, c] (quadrant II), pair 1 real = x[i, c] (quadrant III)
         real va[HE], vb[HE];
 #pragma unroll
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(FftLaunch<real, l, CB>::threads, FftLaunch<rea
             }
         }
     } else if (src_kind == 0) {
-        const size_t ib = (size_t)img * N * N;
+        const size_t ib = (size_t)img * src_stride;
         // column reads: pair 0 imag = x[N-1-i, c] (quadrant II), pair 1 real = x[i, c] (quadrant III)
         real v[F::E];
 #pragma unroll
@@ -301,33 +301,36 @@ template <typename real, int l> constexpr int cols_wide() { return fft_cols<l>(F
 template <typename real, int l> constexpr int cols_narrow() { return imax(1, cols_wide<real, l>() / 4); }
 
 template <typename real, int l, int CB, typename SRC>
-static int launch_pack_cb(int nimg, int src_kind, const void* src, void* Y, const void* roots, cudaStream_t st) {
+static int launch_pack_cb(int nimg, int src_kind, const void* src, long long src_stride, void* Y, const void* roots,
+                          cudaStream_t st) {
     constexpr int N = 1 << (l - 1);
     const size_t smem = pack_smem<real, l, CB>();
     auto kern = pack_fft_kernel<real, l, CB, SRC>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(N / CB, 2, nimg);
     kern<<<grid, CB * FftCfg<l>::TPC, smem, st>>>(nimg, src_kind, reinterpret_cast<const SRC*>(src),
+                                                   src_stride ? src_stride : (long long)N * N,
                                                    reinterpret_cast<cplx<real>*>(Y),
                                                    reinterpret_cast<const cplx<real>*>(roots));
     return launch_status("pack_fft_kernel");
 }
 
 template <typename real, int l, typename SRC>
-static int launch_pack_src(int nimg, int src_kind, const void* src, void* Y, const void* roots, int cols,
-                           cudaStream_t st) {
+static int launch_pack_src(int nimg, int src_kind, const void* src, long long src_stride, void* Y, const void* roots,
+                           int cols, cudaStream_t st) {
     constexpr int W = cols_wide<real, l>(), NW = cols_narrow<real, l>();
-    if (cols == 0 || cols == W) return launch_pack_cb<real, l, W, SRC>(nimg, src_kind, src, Y, roots, st);
-    if (NW != W && cols == NW) return launch_pack_cb<real, l, NW, SRC>(nimg, src_kind, src, Y, roots, st);
+    if (cols == 0 || cols == W) return launch_pack_cb<real, l, W, SRC>(nimg, src_kind, src, src_stride, Y, roots, st);
+    if (NW != W && cols == NW) return launch_pack_cb<real, l, NW, SRC>(nimg, src_kind, src, src_stride, Y, roots, st);
     set_error("pack_fft: %d columns per CTA unsupported (%d or %d at n=%d)", cols, W, NW, l - 1);
     return ADRT_EINVAL;
 }
 
 template <typename real, int l>
-static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, int cols,
-                       cudaStream_t st) {
-    if (src_dtype == ADRT_F64) return launch_pack_src<real, l, double>(nimg, src_kind, src, Y, roots, cols, st);
-    return launch_pack_src<real, l, float>(nimg, src_kind, src, Y, roots, cols, st);
+static int launch_pack(int nimg, int src_kind, int src_dtype, const void* src, long long src_stride, void* Y,
+                       const void* roots, int cols, cudaStream_t st) {
+    if (src_dtype == ADRT_F64)
+        return launch_pack_src<real, l, double>(nimg, src_kind, src, src_stride, Y, roots, cols, st);
+    return launch_pack_src<real, l, float>(nimg, src_kind, src, src_stride, Y, roots, cols, st);
 }
 
 template <typename real, int l, int CB>
@@ -370,9 +373,9 @@ static int launch_unpack(int nimg, const void* Z, void* colpart, void* row0, voi
     }
 
 template <typename real>
-static int pack_t(int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots, int cols,
-                  cudaStream_t st) {
-    ADRT_FFT_CASES(launch_pack, nimg, src_kind, src_dtype, src, Y, roots, cols, st)
+static int pack_t(int n, int nimg, int src_kind, int src_dtype, const void* src, long long src_stride, void* Y,
+                  const void* roots, int cols, cudaStream_t st) {
+    ADRT_FFT_CASES(launch_pack, nimg, src_kind, src_dtype, src, src_stride, Y, roots, cols, st)
     set_error("pack_fft: n=%d unsupported", n);
     return ADRT_EUNSUPPORTED;
 }
@@ -384,16 +387,19 @@ static int unpack_t(int n, int nimg, const void* Z, void* colpart, void* row0, v
     return ADRT_EUNSUPPORTED;
 }
 
-int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-             int cols, cudaStream_t st) {
+int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, long long src_stride, void* Y,
+             const void* roots, int cols, cudaStream_t st) {
+    const long long NN = n >= 1 && n <= 11 ? 1ll << (2 * n) : 0;
     if (n < 1 || n > 11 || nimg < 0 || (src_kind != 0 && src_kind != 1) ||
-        (src_dtype != ADRT_F32 && src_dtype != ADRT_F64) || (nimg && (!src || !Y || !roots))) {
-        set_error("pack_fft: bad arguments (n=%d nimg=%d src_kind=%d src_dtype=%d)", n, nimg, src_kind, src_dtype);
+        (src_dtype != ADRT_F32 && src_dtype != ADRT_F64) || (nimg && (!src || !Y || !roots)) ||
+        (src_stride != 0 && (src_kind != 0 || src_stride < NN || src_stride % 4 != 0))) {
+        set_error("pack_fft: bad arguments (n=%d nimg=%d src_kind=%d src_dtype=%d src_stride=%lld)", n, nimg, src_kind,
+                  src_dtype, src_stride);
         return ADRT_EINVAL;
     }
     if (!nimg) return ADRT_OK;
-    if (dtype == ADRT_F32) return pack_t<float>(n, nimg, src_kind, src_dtype, src, Y, roots, cols, st);
-    if (dtype == ADRT_F64) return pack_t<double>(n, nimg, src_kind, src_dtype, src, Y, roots, cols, st);
+    if (dtype == ADRT_F32) return pack_t<float>(n, nimg, src_kind, src_dtype, src, src_stride, Y, roots, cols, st);
+    if (dtype == ADRT_F64) return pack_t<double>(n, nimg, src_kind, src_dtype, src, src_stride, Y, roots, cols, st);
     set_error("pack_fft: dtype must be F32 or F64");
     return ADRT_EINVAL;
 }

@@ -148,6 +148,26 @@ int image_sum3(int dtype, int n, int nimg, const void* p0, const void* p1, const
     return launch_status("sum3_kernel");
 }
 
+// float-float planes (nimg, 2, N, N), hi then lo per image, to FP64 (nimg, N, N): the result of an inverse whose
+// outer state is kept as float-float
+__global__ void ff_to_f64_kernel(int n, size_t total, const float* __restrict__ x, double* __restrict__ out) {
+    const size_t NN = (size_t)1 << (2 * n);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t img = i >> (2 * n), e = i & (NN - 1);
+        const float* p = x + img * 2 * NN + e;
+        out[i] = (double)p[0] + (double)p[NN];
+    }
+}
+
+int ff_to_f64(int n, int nimg, const float* x, double* out, cudaStream_t st) {
+    if (n < 1 || n > 11 || nimg < 0) { set_error("ff_to_f64: bad arguments (n=%d nimg=%d)", n, nimg); return ADRT_EINVAL; }
+    const size_t total = (size_t)nimg << (2 * n);
+    if (!total) return ADRT_OK;
+    if (!x || !out) { set_error("ff_to_f64: null pointer"); return ADRT_EINVAL; }
+    ff_to_f64_kernel<<<grid_for(total), 256, 0, st>>>(n, total, x, out);
+    return launch_status("ff_to_f64_kernel");
+}
+
 int image_g1_step(int dtype, int n, int nimg, const void* s, const void* x, const void* xp, void* xn, double om_a, double om_1,
                   double a0, cudaStream_t st) {
     if (!img_args_ok(dtype, n, nimg, "g1_step")) return ADRT_EINVAL;

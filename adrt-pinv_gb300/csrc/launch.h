@@ -8,8 +8,8 @@ namespace adrt {
 int device_sm_count();
 int rows_run(const adrt_row_job* J, int power_iters, double power_safety, double* power_out, cudaStream_t st);
 int twiddle_table(int dtype, int n, int K, const double* z, void* tab, cudaStream_t st);
-int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-             int cols, cudaStream_t st);
+int pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, long long src_stride, void* Y,
+             const void* roots, int cols, cudaStream_t st);
 int ifft_unpack(int dtype, int n, int nimg, const void* Z, void* colpart, void* row0, void* row3, const void* roots,
                 int cols, cudaStream_t st);
 int image_resid(int dtype, int n, int nimg, int ydtype, const void* y, const void* p0, const void* p1, const void* p2,
@@ -32,6 +32,10 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
                const void* p2, const double* x, const double* xp, double* xn, double om_a, double om_1, double a0,
                int precond, int g1_deg, const double* g1_coef, const double* om_img, int band, cudaStream_t st);
 int outer_step_max_n(int dtype);
+int outer_step_ff(int n, int nimg, const float* y, const float* p0, const float* p1, const float* p2, const float* x,
+                  const float* xp, float* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
+                  const double* g1_coef, const double* om_img, int band, cudaStream_t st);
+int ff_to_f64(int n, int nimg, const float* x, double* out, cudaStream_t st);
 int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
                void* Zd, int* err, int use_tc, int tile, cudaStream_t st);
 int cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, cudaStream_t st);

@@ -57,6 +57,12 @@ struct OuterStepArgs {
     const double* x;
     const double* xp;
     double* xn;
+    // the float-float form (register-resident kernel only): y in FP32 (nimg, N, N); x, xp, xn as (nimg, 2, N, N)
+    // FP32 planes, hi then lo per image (value = hi + lo)
+    const float* yf;
+    const float* xf;
+    const float* xpf;
+    float* xnf;
     double om_a, om_1, a0;
     const double* om_img;  // nullable: per-image (om_a, om_1) pairs replacing om_a, om_1 (slot-level serving)
     int precond;  // 0 none, 1 g1, 2 lorr
@@ -200,135 +206,185 @@ __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepA
     }
 }
 
-// ------------------------------------------------------------------ register-resident form (FP32 stencil and partial
-// images, 64 <= N <= 512). Thread (g, u) of a CTA owns the column pair (2u, 2u + 1) on the OSR_R rows of row group g
-// (rows row0 .. row0 + OSR_R - 1 of the image): its residual, both stencil iterates and its outer update stay in
-// registers for the whole launch. A stencil step finds the pair column j ^ 1 and the rows above and below inside the
-// thread, and the columns 2u - 1 and 2u + 2 in the neighbouring lanes (warp shuffles). Only what crosses a thread
-// boundary goes through shared memory, once per step: the first and last row of every row group (halo rows, read by
-// the group above / below, in this CTA or over distributed shared memory in the neighbouring CTA of the image's
-// cluster) and the first and last column of every warp (read by the edge lanes of the neighbouring warps). The
-// buffers alternate between two copies, so one cluster barrier per step orders every write before its reads and
-// every read before the next overwrite. The arithmetic is the shared-memory kernel's, term for term.
-constexpr int OSR_R = 16;
+// CPT consecutive FP32 values of a row (CPT even; 16-byte accesses where CPT is a multiple of 4)
+template <int CPT> __device__ __forceinline__ void ld_row(const float* p, float (&v)[CPT]) {
+    if constexpr (CPT % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < CPT / 4; ++q) {
+            const float4 t = *reinterpret_cast<const float4*>(p + 4 * q);
+            v[4 * q] = t.x; v[4 * q + 1] = t.y; v[4 * q + 2] = t.z; v[4 * q + 3] = t.w;
+        }
+    } else {
+#pragma unroll
+        for (int q = 0; q < CPT / 2; ++q) {
+            const float2 t = *reinterpret_cast<const float2*>(p + 2 * q);
+            v[2 * q] = t.x; v[2 * q + 1] = t.y;
+        }
+    }
+}
+template <int CPT> __device__ __forceinline__ void st_row(float* p, const float (&v)[CPT]) {
+    if constexpr (CPT % 4 == 0) {
+#pragma unroll
+        for (int q = 0; q < CPT / 4; ++q)
+            *reinterpret_cast<float4*>(p + 4 * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+    } else {
+#pragma unroll
+        for (int q = 0; q < CPT / 2; ++q) *reinterpret_cast<float2*>(p + 2 * q) = make_float2(v[2 * q], v[2 * q + 1]);
+    }
+}
 
-template <int n, int BAND>
-__global__ void __launch_bounds__((1 << n) / 2 * (BAND / OSR_R), (1 << n) <= 256 ? 2 : 1)
+// ------------------------------------------------------------------ register-resident form (FP32 stencil and partial
+// images, 64 <= N <= 512). Warp w of a CTA owns a strip of R = 1024 / N rows spanning the whole row: lane l holds
+// columns l CPT .. l CPT + CPT - 1 (CPT = N / 32) of those rows, so its residual, both stencil iterates and its outer
+// update stay in registers for the whole launch, and every 2x2 cell (row pair, column pair) of the G_1 stencil lies
+// inside one thread. Per cell, with S the cell's sum, the stencil is
+//     (G_1 c)(i, j) = 6 c(i, j) + 2 S + c(i', j') + c(i'', j^1)       i'' = the other row of the pair, j' = the column
+//                                                                       beside the cell on i''; i' = the row beside
+//                                                                       the cell on column j^1
+// (the K term along rows and the transposed term along columns of fasthybrid.py:81-99, regrouped). The only values
+// from outside a thread are the columns beside its first and last column (warp shuffles; zero at the image border)
+// and, for the strip's first and last rows, the rows above and below the strip: other warps publish those into shared
+// memory once per step (the strip above / below in the neighbouring CTA of the image's cluster through distributed
+// shared memory). The cluster barrier is split: a step is computed without the strip-boundary terms while the
+// barrier completes, then the boundary terms are read and applied (the step is linear in them). Two copies of the
+// boundary buffer alternate, so each write is ordered after the previous step's reads of that copy.
+template <int n, int BAND, bool FF>
+__global__ void __launch_bounds__(32 * (BAND / (1024 >> n)), (1 << n) <= 256 ? 2 : 1)
     outer_step_reg_kernel(const OuterStepArgs A) {
     constexpr int N = 1 << n;
-    constexpr int R = OSR_R;
-    constexpr int G = BAND / R;   // row groups per CTA
-    constexpr int TPR = N / 2;    // threads per row group
-    constexpr int NW = TPR / 32;  // warps per row group
-    constexpr int CL = N / BAND;  // CTAs per image (the cluster)
-    static_assert(TPR % 32 == 0 && BAND % R == 0 && R % 2 == 0, "whole warps per row group, row pairs per group");
-    __shared__ __align__(16) float halo[2][G][2][N];  // [copy][group][first / last row][column]
-    __shared__ float edge[2][G][NW][2][R];            // [copy][group][warp][first / last column][row]
+    constexpr int CPT = N / 32;    // columns per thread
+    constexpr int R = 32 / CPT;    // rows per strip (warp)
+    constexpr int W = BAND / R;    // strips per CTA
+    constexpr int CL = N / BAND;   // CTAs per image (the cluster)
+    constexpr int HC = W * 2 * N;  // floats per copy of the boundary buffer [strip][first / last row][column]
+    static_assert(CPT >= 2 && CPT % 2 == 0 && R % 2 == 0 && BAND % R == 0, "cells inside a thread, row pairs per strip");
+    extern __shared__ __align__(16) float bnd[];  // [2][W][2][N]
     cg::cluster_group cluster = cg::this_cluster();
     const int rank = (int)cluster.block_rank();
     const int img = blockIdx.x / CL;
-    const int g = threadIdx.x / TPR, u = threadIdx.x - g * TPR;
-    const int lane = threadIdx.x & 31, wg = u >> 5;
-    const size_t gbase = (size_t)img * N * N + (size_t)(rank * BAND + g * R) * N + 2 * u;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int j0 = lane * CPT;
+    const size_t gbase = (size_t)img * N * N + (size_t)(rank * BAND + w * R) * N + j0;
     constexpr unsigned FULL = 0xffffffffu;
 
-    // residual: the partial images summed in FP32, the difference in FP64, rounded to FP32
-    float2 sv[R];
+    // residual: the partial images summed in FP32, the difference in FP64 rounded to FP32 (FP64 y), or in FP32 (FP32
+    // y: the same value, since the exact difference of two FP32 numbers is rounded once either way)
+    float s[R][CPT];
     {
         const float* p0 = reinterpret_cast<const float*>(A.p0);
         const float* p1 = reinterpret_cast<const float*>(A.p1);
         const float* p2 = reinterpret_cast<const float*>(A.p2);
 #pragma unroll
-        for (int r0 = 0; r0 < R; r0 += 8) {
-            float2 t[8];
-            double2 yv[8];
+        for (int r = 0; r < R; ++r) {
+            const size_t gi = gbase + (size_t)r * N;
+            double2 yv[CPT / 2];
+            float yfv[CPT];
+            if constexpr (FF) {
+                ld_row<CPT>(A.yf + gi, yfv);
+            } else {
 #pragma unroll
-            for (int r = 0; r < 8; ++r) {
-                const size_t gi = gbase + (size_t)(r0 + r) * N;
-                t[r] = make_float2(0.f, 0.f);
-                if (p0) {
-                    const float2 a = *reinterpret_cast<const float2*>(p0 + gi);
-                    const float2 b = *reinterpret_cast<const float2*>(p1 + gi);
-                    const float2 c = *reinterpret_cast<const float2*>(p2 + gi);
-                    t[r] = make_float2((a.x + b.x) + c.x, (a.y + b.y) + c.y);
+                for (int q = 0; q < CPT / 2; ++q) yv[q] = *reinterpret_cast<const double2*>(A.y + gi + 2 * q);
+            }
+            float t[CPT];
+#pragma unroll
+            for (int q = 0; q < CPT; ++q) t[q] = 0.f;
+            if (p0) {
+#pragma unroll
+                for (int q = 0; q < CPT / 2; ++q) {
+                    const float2 a = *reinterpret_cast<const float2*>(p0 + gi + 2 * q);
+                    const float2 b = *reinterpret_cast<const float2*>(p1 + gi + 2 * q);
+                    const float2 c = *reinterpret_cast<const float2*>(p2 + gi + 2 * q);
+                    t[2 * q] = (a.x + b.x) + c.x;
+                    t[2 * q + 1] = (a.y + b.y) + c.y;
                 }
-                yv[r] = *reinterpret_cast<const double2*>(A.y + gi);
             }
 #pragma unroll
-            for (int r = 0; r < 8; ++r)
-                sv[r0 + r] = make_float2((float)(yv[r].x - (double)t[r].x), (float)(yv[r].y - (double)t[r].y));
+            for (int q = 0; q < CPT / 2; ++q) {
+                if constexpr (FF) {
+                    s[r][2 * q] = yfv[2 * q] - t[2 * q];
+                    s[r][2 * q + 1] = yfv[2 * q + 1] - t[2 * q + 1];
+                } else {
+                    s[r][2 * q] = (float)(yv[q].x - (double)t[2 * q]);
+                    s[r][2 * q + 1] = (float)(yv[q].y - (double)t[2 * q + 1]);
+                }
+            }
         }
     }
 
-    float2 cA[R], cB[R];
+    float cA[R][CPT], cB[R][CPT];
     bool in_b = false;  // the result of the preconditioner is in cB (else in cA)
     if (A.precond == 1) {
-        float* halo0 = &halo[0][0][0][0];
-        const float* up = rank > 0 ? cluster.map_shared_rank(halo0, rank - 1) : nullptr;
-        const float* dn = rank < CL - 1 ? cluster.map_shared_rank(halo0, rank + 1) : nullptr;
-        constexpr int HCOPY = G * 2 * N;  // floats per halo copy
-        // publish the boundary of iterate v into copy b
-        auto publish = [&](const float2 (&v)[R], int b) {
-            *reinterpret_cast<float2*>(&halo[b][g][0][2 * u]) = v[0];
-            *reinterpret_cast<float2*>(&halo[b][g][1][2 * u]) = v[R - 1];
-            if (lane == 0 || lane == 31) {
+        const float* up = rank > 0 ? cluster.map_shared_rank(bnd, rank - 1) : nullptr;
+        const float* dn = rank < CL - 1 ? cluster.map_shared_rank(bnd, rank + 1) : nullptr;
+        // the strip's first and last rows of iterate v into copy b, then arrive at the cluster barrier
+        auto publish = [&](const float (&v)[R][CPT], int b) {
+            float* f = bnd + b * HC + (w * 2) * N + j0;
 #pragma unroll
-                for (int r = 0; r < R; ++r) edge[b][g][wg][lane == 31][r] = lane == 31 ? v[r].y : v[r].x;
+            for (int q = 0; q < CPT / 2; ++q) {
+                *reinterpret_cast<float2*>(f + 2 * q) = make_float2(v[0][2 * q], v[0][2 * q + 1]);
+                *reinterpret_cast<float2*>(f + N + 2 * q) = make_float2(v[R - 1][2 * q], v[R - 1][2 * q + 1]);
             }
-            cluster.sync();
+            asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
         };
-        // one Chebyshev step p <- c + om_a (s - G1 c) + om_1 (c - p), the boundary of c read from copy b
-        auto step = [&](const float2 (&c)[R], float2 (&p)[R], float om_a, float om_1, int b) {
-            // the pair columns of the rows above and below the group (zero beyond the image)
-            float2 top = make_float2(0.f, 0.f), bot = make_float2(0.f, 0.f);
-            if (g > 0) top = *reinterpret_cast<const float2*>(&halo[b][g - 1][1][2 * u]);
-            else if (up) top = *reinterpret_cast<const float2*>(up + b * HCOPY + ((G - 1) * 2 + 1) * N + 2 * u);
-            if (g < G - 1) bot = *reinterpret_cast<const float2*>(&halo[b][g + 1][0][2 * u]);
-            else if (dn) bot = *reinterpret_cast<const float2*>(dn + b * HCOPY + 2 * u);
-            // edge lanes: lane 0 takes column 2u - 1 from the last column of the warp before, lane 31 column
-            // 2u + 2 from the first column of the warp after (zero at the image's first / last column)
-            const float* ecol = lane == 0 ? &edge[b][g][wg > 0 ? wg - 1 : 0][1][0]
-                                          : &edge[b][g][wg < NW - 1 ? wg + 1 : NW - 1][0][0];
-            const bool zl = u == 0, zr = u == TPR - 1;
-            float lf[R], rt[R];  // columns 2u - 1 and 2u + 2 of every row
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                const float ev = ecol[r];
-                const float l = __shfl_up_sync(FULL, c[r].y, 1);
-                const float q = __shfl_down_sync(FULL, c[r].x, 1);
-                lf[r] = zl ? 0.f : (lane == 0 ? ev : l);
-                rt[r] = zr ? 0.f : (lane == 31 ? ev : q);
-            }
+        // one Chebyshev step p <- c + om_a (s - G1 c) + om_1 (c - p); the boundary of c is in copy b
+        auto step = [&](const float (&c)[R][CPT], float (&p)[R][CPT], float om_a, float om_1, int b) {
 #pragma unroll
             for (int m = 0; m < R / 2; ++m) {
                 const int r0 = 2 * m, r1 = r0 + 1;
-                const float2 c0 = c[r0], c1 = c[r1];
-                const float2 qm = r0 > 0 ? c[r0 - 1] : top;  // row above, both columns
-                const float2 qp = r1 < R - 1 ? c[r1 + 1] : bot;
-                // column 2u (pair column 2u + 1; left neighbour lf, right neighbour the pair column)
-                const float b0x = (2.f * c1.x + lf[r1]) + c1.y;
-                const float b1x = (2.f * c0.x + lf[r0]) + c0.y;
-                const float a0x = (2.f * c0.y + qm.y) + c1.y;
-                const float a1x = (2.f * c1.y + c0.y) + qp.y;
-                // column 2u + 1 (pair column 2u; left neighbour the pair column, right neighbour rt)
-                const float b0y = (2.f * c1.y + c1.x) + rt[r1];
-                const float b1y = (2.f * c0.y + c0.x) + rt[r0];
-                const float a0y = (2.f * c0.x + qm.x) + c1.x;
-                const float a1y = (2.f * c1.x + c0.x) + qp.x;
-                const float g0x = (8.f * c0.x + a0x) + b0x, g1x = (8.f * c1.x + a1x) + b1x;
-                const float g0y = (8.f * c0.y + a0y) + b0y, g1y = (8.f * c1.y + a1y) + b1y;
-                p[r0].x = (c0.x + om_a * (sv[r0].x - g0x)) + om_1 * (c0.x - p[r0].x);
-                p[r0].y = (c0.y + om_a * (sv[r0].y - g0y)) + om_1 * (c0.y - p[r0].y);
-                p[r1].x = (c1.x + om_a * (sv[r1].x - g1x)) + om_1 * (c1.x - p[r1].x);
-                p[r1].y = (c1.y + om_a * (sv[r1].y - g1y)) + om_1 * (c1.y - p[r1].y);
+                // the columns beside the thread's first and last column, on both rows of the pair
+                const float l0 = __shfl_up_sync(FULL, c[r0][CPT - 1], 1), l1 = __shfl_up_sync(FULL, c[r1][CPT - 1], 1);
+                const float q0 = __shfl_down_sync(FULL, c[r0][0], 1), q1 = __shfl_down_sync(FULL, c[r1][0], 1);
+                const float L0 = lane == 0 ? 0.f : l0, L1 = lane == 0 ? 0.f : l1;
+                const float R0 = lane == 31 ? 0.f : q0, R1 = lane == 31 ? 0.f : q1;
+#pragma unroll
+                for (int v = 0; v < CPT / 2; ++v) {
+                    const int a = 2 * v, bb = a + 1;
+                    const float c00 = c[r0][a], c01 = c[r0][bb], c10 = c[r1][a], c11 = c[r1][bb];
+                    const float t = 2.f * ((c00 + c01) + (c10 + c11));
+                    float g00 = fmaf(6.f, c00, t), g01 = fmaf(6.f, c01, t);
+                    float g10 = fmaf(6.f, c10, t), g11 = fmaf(6.f, c11, t);
+                    if (r0 > 0) {  // the row above the pair, pair column (the strip's first row: deferred)
+                        g00 += c[r0 - 1][bb];
+                        g01 += c[r0 - 1][a];
+                    }
+                    if (r1 < R - 1) {  // the row below
+                        g10 += c[r1 + 1][bb];
+                        g11 += c[r1 + 1][a];
+                    }
+                    g00 += v > 0 ? c[r1][a - 1] : L1;  // beside the cell, on the other row of the pair
+                    g10 += v > 0 ? c[r0][a - 1] : L0;
+                    g01 += v < CPT / 2 - 1 ? c[r1][bb + 1] : R1;
+                    g11 += v < CPT / 2 - 1 ? c[r0][bb + 1] : R0;
+                    p[r0][a] = (c00 + om_a * (s[r0][a] - g00)) + om_1 * (c00 - p[r0][a]);
+                    p[r0][bb] = (c01 + om_a * (s[r0][bb] - g01)) + om_1 * (c01 - p[r0][bb]);
+                    p[r1][a] = (c10 + om_a * (s[r1][a] - g10)) + om_1 * (c10 - p[r1][a]);
+                    p[r1][bb] = (c11 + om_a * (s[r1][bb] - g11)) + om_1 * (c11 - p[r1][bb]);
+                }
+            }
+            asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+            // the rows above and below the strip (zero beyond the image): G_1 c gains c(above, j^1) on the first
+            // row and c(below, j^1) on the last, so p loses om_a times those
+            const float* fa = w > 0 ? bnd + b * HC + ((w - 1) * 2 + 1) * N
+                                    : (up ? up + b * HC + ((W - 1) * 2 + 1) * N : nullptr);
+            const float* fb = w < W - 1 ? bnd + b * HC + ((w + 1) * 2) * N : (dn ? dn + b * HC : nullptr);
+#pragma unroll
+            for (int q = 0; q < CPT / 2; ++q) {
+                const float2 ta = fa ? *reinterpret_cast<const float2*>(fa + j0 + 2 * q) : make_float2(0.f, 0.f);
+                const float2 tb = fb ? *reinterpret_cast<const float2*>(fb + j0 + 2 * q) : make_float2(0.f, 0.f);
+                p[0][2 * q] = fmaf(-om_a, ta.y, p[0][2 * q]);
+                p[0][2 * q + 1] = fmaf(-om_a, ta.x, p[0][2 * q + 1]);
+                p[R - 1][2 * q] = fmaf(-om_a, tb.y, p[R - 1][2 * q]);
+                p[R - 1][2 * q + 1] = fmaf(-om_a, tb.x, p[R - 1][2 * q + 1]);
             }
         };
         const float a0 = (float)A.g1_a0;
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            cA[r] = make_float2(a0 * sv[r].x, a0 * sv[r].y);
-            cB[r] = make_float2(0.f, 0.f);
-        }
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int q = 0; q < CPT; ++q) {
+                cA[r][q] = a0 * s[r][q];
+                cB[r][q] = 0.f;
+            }
         publish(cA, 0);
         int k = 1;
         for (; k + 1 < A.g1_deg; k += 2) {
@@ -342,47 +398,107 @@ __global__ void __launch_bounds__((1 << n) / 2 * (BAND / OSR_R), (1 << n) <= 256
             publish(cB, k & 1);
             in_b = true;
         }
+        // the last arrival's wait: no CTA leaves while a neighbour may still read its boundary rows
+        asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
     } else if (A.precond == 2) {
-        // (s - Pi s)/4 + Pi s/12, Pi the mean of the 2x2 cell (rows r0, r0 + 1; columns 2u, 2u + 1)
+        // (s - Pi s)/4 + Pi s/12, Pi the mean of the 2x2 cell
 #pragma unroll
-        for (int r0 = 0; r0 < R; r0 += 2) {
-            const float mu = ((sv[r0].x + sv[r0].y) + (sv[r0 + 1].x + sv[r0 + 1].y)) * 0.25f;
+        for (int r0 = 0; r0 < R; r0 += 2)
 #pragma unroll
-            for (int q = 0; q < 2; ++q) {
-                const float2 v = sv[r0 + q];
-                cA[r0 + q] = make_float2((v.x - mu) * 0.25f + mu / 12.f, (v.y - mu) * 0.25f + mu / 12.f);
+            for (int a = 0; a < CPT; a += 2) {
+                const float mu = ((s[r0][a] + s[r0][a + 1]) + (s[r0 + 1][a] + s[r0 + 1][a + 1])) * 0.25f;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const int r = r0 + (q >> 1), c = a + (q & 1);
+                    cA[r][c] = (s[r][c] - mu) * 0.25f + mu / 12.f;
+                }
             }
-        }
     } else {
 #pragma unroll
-        for (int r = 0; r < R; ++r) cA[r] = sv[r];
+        for (int r = 0; r < R; ++r)
+#pragma unroll
+            for (int q = 0; q < CPT; ++q) cA[r][q] = s[r][q];
     }
 
-    // outer update in FP64
+    // outer update: in FP64 (FP64 state), or in float-float on the FP32 pipe (float-float state): the step
+    // om_a r + om_1 (x - x_prev) in FP32 with the coefficients carried as hi + lo, added to x with an exact
+    // two-sum, so the state keeps about 48 bits while no FP64 instruction runs (the FP64 pipe of this GPU is a small
+    // fraction of its FP32 pipe)
     const double oa = A.om_img ? A.om_img[2 * img] : A.om_a;
     const double o1 = A.om_img ? A.om_img[2 * img + 1] : A.om_1;
+    if constexpr (FF) {
+        const float oah = (float)oa, oal = (float)(oa - (double)oah);
+        const float o1h = (float)o1, o1l = (float)(o1 - (double)o1h);
+        const float a0h = (float)A.a0, a0l = (float)(A.a0 - (double)a0h);
+        const size_t fo = gbase + (size_t)img * N * N;  // hi plane of this thread's first row; lo plane N^2 further
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const size_t gi = fo + (size_t)r * N;
+            float rv[CPT], hv[CPT], lv[CPT];
+#pragma unroll
+            for (int q = 0; q < CPT; ++q) rv[q] = in_b ? cB[r][q] : cA[r][q];
+            if (!A.xf) {
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) {
+                    const float h = a0h * rv[q];
+                    const float l = fmaf(a0h, rv[q], -h) + a0l * rv[q];
+                    hv[q] = h + l;
+                    lv[q] = l - (hv[q] - h);
+                }
+            } else {
+                float xh[CPT], xl[CPT], ph[CPT], pl[CPT];
+                ld_row<CPT>(A.xf + gi, xh);
+                ld_row<CPT>(A.xf + gi + (size_t)N * N, xl);
+                if (A.xpf) {
+                    ld_row<CPT>(A.xpf + gi, ph);
+                    ld_row<CPT>(A.xpf + gi + (size_t)N * N, pl);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < CPT; ++q) ph[q] = pl[q] = 0.f;
+                }
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) {
+                    const float d = (xh[q] - ph[q]) + (xl[q] - pl[q]);
+                    const float del = fmaf(oah, rv[q], fmaf(o1h, d, fmaf(oal, rv[q], o1l * d)));
+                    const float sh = xh[q] + del, bb = sh - xh[q];
+                    const float lo = ((xh[q] - (sh - bb)) + (del - bb)) + xl[q];
+                    hv[q] = sh + lo;
+                    lv[q] = lo - (hv[q] - sh);
+                }
+            }
+            st_row<CPT>(A.xnf + gi, hv);
+            st_row<CPT>(A.xnf + gi + (size_t)N * N, lv);
+        }
+        return;
+    }
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const size_t gi = gbase + (size_t)r * N;
-        const float2 rv = in_b ? cB[r] : cA[r];
-        const double r0 = (double)rv.x, r1 = (double)rv.y;
-        double2 out;
-        if (!A.x) {
-            out = make_double2(A.a0 * r0, A.a0 * r1);
-        } else {
-            const double2 xv = *reinterpret_cast<const double2*>(A.x + gi);
-            const double2 pv = A.xp ? *reinterpret_cast<const double2*>(A.xp + gi) : make_double2(0.0, 0.0);
-            out = make_double2(xv.x + oa * r0 + o1 * (xv.x - pv.x), xv.y + oa * r1 + o1 * (xv.y - pv.y));
+#pragma unroll
+        for (int q = 0; q < CPT / 2; ++q) {
+            const double r0 = (double)(in_b ? cB[r][2 * q] : cA[r][2 * q]);
+            const double r1 = (double)(in_b ? cB[r][2 * q + 1] : cA[r][2 * q + 1]);
+            double2 out;
+            if (!A.x) {
+                out = make_double2(A.a0 * r0, A.a0 * r1);
+            } else {
+                const double2 xv = *reinterpret_cast<const double2*>(A.x + gi + 2 * q);
+                const double2 pv = A.xp ? *reinterpret_cast<const double2*>(A.xp + gi + 2 * q) : make_double2(0.0, 0.0);
+                out = make_double2(xv.x + oa * r0 + o1 * (xv.x - pv.x), xv.y + oa * r1 + o1 * (xv.y - pv.y));
+            }
+            *reinterpret_cast<double2*>(A.xn + gi + 2 * q) = out;
         }
-        *reinterpret_cast<double2*>(A.xn + gi) = out;
     }
 }
 
-template <int n, int BAND>
+template <int n, int BAND, bool FF>
 static int launch_os_reg(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     constexpr int N = 1 << n;
     constexpr int CL = N / BAND;
-    auto kern = outer_step_reg_kernel<n, BAND>;
+    constexpr int W = BAND / (1024 / N);
+    const size_t smem = 2 * (size_t)W * 2 * N * sizeof(float);
+    auto kern = outer_step_reg_kernel<n, BAND, FF>;
+    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     if (CL > 8) {
         if (int rc = cuda_status(cudaFuncSetAttribute((const void*)kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1),
                                  "outer_step cluster attribute"))
@@ -390,8 +506,8 @@ static int launch_os_reg(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(nimg * CL);
-    cfg.blockDim = dim3(N / 2 * (BAND / OSR_R));
-    cfg.dynamicSmemBytes = 0;
+    cfg.blockDim = dim3(32 * W);
+    cfg.dynamicSmemBytes = smem;
     cfg.stream = st;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeClusterDimension;
@@ -468,22 +584,23 @@ static int dispatch_os(int n, const OuterStepArgs& A, int nimg, int band, cudaSt
 }
 
 // register-resident form, FP32 stencil and partial images, n = 6..9; bands as in launch_os
-template <int n>
+template <int n, bool FF>
 static int launch_os_reg_auto(const OuterStepArgs& A, int nimg, int band, cudaStream_t st) {
     constexpr int N = 1 << n;
     const bool b16 = band ? band == 16 : (long)nimg * (N / 32) < device_sm_count();
     if constexpr (N / 16 <= 16) {
-        if (b16) return launch_os_reg<n, 16>(A, nimg, st);
+        if (b16) return launch_os_reg<n, 16, FF>(A, nimg, st);
     }
-    return launch_os_reg<n, 32>(A, nimg, st);
+    return launch_os_reg<n, 32, FF>(A, nimg, st);
 }
 
+template <bool FF>
 static int dispatch_os_reg(int n, const OuterStepArgs& A, int nimg, int band, cudaStream_t st) {
     switch (n) {
-        case 6: return launch_os_reg_auto<6>(A, nimg, band, st);
-        case 7: return launch_os_reg_auto<7>(A, nimg, band, st);
-        case 8: return launch_os_reg_auto<8>(A, nimg, band, st);
-        case 9: return launch_os_reg_auto<9>(A, nimg, band, st);
+        case 6: return launch_os_reg_auto<6, FF>(A, nimg, band, st);
+        case 7: return launch_os_reg_auto<7, FF>(A, nimg, band, st);
+        case 8: return launch_os_reg_auto<8, FF>(A, nimg, band, st);
+        case 9: return launch_os_reg_auto<9, FF>(A, nimg, band, st);
     }
     set_error("outer_step: no register-resident form for n=%d", n);
     return ADRT_EUNSUPPORTED;
@@ -521,7 +638,7 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
     // FP32 stencil on FP32 partial images: the register-resident form where it exists, unless the shared-memory
     // form is asked for
     if (!shared_form && dtype == ADRT_F32 && parts_dtype == ADRT_F32 && n >= 6 && n <= 9)
-        return dispatch_os_reg(n, A, nimg, band, st);
+        return dispatch_os_reg<false>(n, A, nimg, band, st);
     // instantiated pairs: FP32 partial images with any stencil type, FP64 partial images with the FP64 stencil
     if (parts_dtype == ADRT_F32) {
         switch (dtype) {
@@ -533,6 +650,32 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
     if (dtype == ADRT_F64) return dispatch_os<double, double>(n, A, nimg, band, st);
     set_error("outer_step: FP64 partial images take the FP64 stencil only");
     return ADRT_EUNSUPPORTED;
+}
+
+// the float-float state form: FP32 stencil and partial images, y FP32, x / x_prev / x_new as float-float planes
+int outer_step_ff(int n, int nimg, const float* y, const float* p0, const float* p1, const float* p2, const float* x,
+                  const float* xp, float* xn, double om_a, double om_1, double a0, int precond, int g1_deg,
+                  const double* g1_coef, const double* om_img, int band, cudaStream_t st) {
+    if (n < 6 || n > 9 || nimg < 0 || precond < 0 || precond > 2 ||
+        (precond == 1 && (g1_deg < 1 || g1_deg > OS_MAX_STEPS || !g1_coef)) || (p0 && (!p1 || !p2)) ||
+        (band != 0 && band != 16 && band != 32)) {
+        set_error("outer_step_ff: bad arguments (n=%d precond=%d deg=%d band=%d; n must be 6..9)", n, precond, g1_deg,
+                  band);
+        return ADRT_EINVAL;
+    }
+    if (!nimg) return ADRT_OK;
+    if (!y || !xn || (om_img && !x)) { set_error("outer_step_ff: null pointer"); return ADRT_EINVAL; }
+    OuterStepArgs A = {};
+    A.yf = y; A.p0 = p0; A.p1 = p1; A.p2 = p2; A.xf = x; A.xpf = xp; A.xnf = xn;
+    A.om_a = om_a; A.om_1 = om_1; A.a0 = a0; A.om_img = om_img; A.precond = precond; A.g1_deg = g1_deg;
+    if (precond == 1) {
+        A.g1_a0 = g1_coef[0];
+        for (int k = 1; k < g1_deg; ++k) {
+            A.g1_om_a[k - 1] = g1_coef[2 * k - 1];
+            A.g1_om_1[k - 1] = g1_coef[2 * k];
+        }
+    }
+    return dispatch_os_reg<true>(n, A, nimg, band, st);
 }
 
 }  // namespace adrt

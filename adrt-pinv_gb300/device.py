@@ -338,7 +338,7 @@ def ops_unfused(ops):
 class Pipeline:
     """Every device buffer for one (plan, batch size, precision)."""
 
-    def __init__(self, plan: Plan, batch, precision="fp32", device="cuda", stencil_precision=None):
+    def __init__(self, plan: Plan, batch, precision="fp32", device="cuda", stencil_precision=None, state="auto"):
         if precision not in PRECISIONS:
             raise ValueError(f"precision must be one of {tuple(PRECISIONS)}")
         C.load()
@@ -357,8 +357,20 @@ class Pipeline:
         dev = self.device
         self.Y = torch.empty((B, 2 * L, N), dtype=_cdtype(self.real), device=dev)
         self.parts = torch.empty((3, B, N, N), dtype=self.real, device=dev)
-        self.xs = [torch.empty((B, N, N), dtype=self.outer_real, device=dev) for _ in range(3)]
-        self.y = torch.empty((B, N, N), dtype=self.outer_real, device=dev)
+        # the outer state: FP64 images, or (where the register-resident fused outer step runs: FP32 rows and
+        # stencil, 64 <= N <= 512) float-float planes (B, 2, N, N), hi then lo per image, with y in FP32 (it is an
+        # FP32 sum of the partial images either way) and the FP64 result converted once at the end of an apply
+        if state not in ("auto", "fp64"):
+            raise ValueError("state must be 'auto' (float-float where the register-resident outer step runs) or 'fp64'")
+        self.ff_state = state == "auto" and Pipeline.ff_state_for(plan, precision, self.stencil_precision)
+        if self.ff_state:
+            self.xs = [torch.empty((B, 2, N, N), dtype=torch.float32, device=dev) for _ in range(3)]
+            self.y = torch.empty((B, N, N), dtype=torch.float32, device=dev)
+            self.x64 = torch.empty((B, N, N), dtype=torch.float64, device=dev)
+        else:
+            self.xs = [torch.empty((B, N, N), dtype=self.outer_real, device=dev) for _ in range(3)]
+            self.y = torch.empty((B, N, N), dtype=self.outer_real, device=dev)
+            self.x64 = None
         self.s = torch.empty((B, N, N), dtype=self.stencil_real, device=dev)
         self.st = [torch.empty((B, N, N), dtype=self.stencil_real, device=dev) for _ in range(3)]
         self.ops = _op_lists(plan)
@@ -385,6 +397,7 @@ class Pipeline:
         q.parts = self.parts[:, :b]
         q.xs = [x[:b] for x in self.xs]
         q.y = self.y[:b]
+        q.x64 = None if self.x64 is None else self.x64[:b]
         q.s = self.s[:b]
         q.st = [x[:b] for x in self.st]
         q.timer = None
@@ -405,22 +418,19 @@ class Pipeline:
         self.timer.append((name, e0, e1))
 
     def packed_image(self, x, ops):
-        """fastops._packed with strips Tq(q, E x): x (B, N, N) real on device -> self.parts."""
-        p, st = self.plan, C.stream_handle()
-        self._timed("pack_image", lambda: C.call("adrt_pack_fft", self._codes(), p.n, self.B, 0, C.dtype_code(x.dtype),
-                                                 C.ptr(x), C.ptr(self.Y), C.ptr(self.tables.roots), self.fft_cols,
-                                                 st))
+        """fastops._packed with strips Tq(q, E x): x (B, N, N) real, or float-float planes (B, 2, N, N), on device
+        -> self.parts."""
+        st = C.stream_handle()
+        self._timed("pack_image", lambda: self.pack(x, sino=False))
         self.tables.run(self.Y, ops)
         self._unpack(st)
         return self.parts
 
     def packed_sino(self, b, ops):
         """fastops._packed with strips iota(b_q): b (B, 4, 2N-1, N) real on device -> self.parts."""
-        p, st = self.plan, C.stream_handle()
-        C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1, C.dtype_code(b.dtype), C.ptr(b), C.ptr(self.Y),
-               C.ptr(self.tables.roots), self.fft_cols, st)
+        self.pack(b, sino=True)
         self.tables.run(self.Y, ops)
-        self._unpack(st)
+        self._unpack(C.stream_handle())
         return self.parts
 
     def _unpack(self, st):
@@ -470,8 +480,9 @@ class Pipeline:
         return pair and self.plan.n <= C.load().adrt_outer_step_max_n(self.stencil_code)
 
     def fused_outer_step(self, y, with_parts, x, x_prev, x_new, om_a, om_1, a0, om_img=None):
-        """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step); om_img (device
-        (B, 2) FP64, optional): per-image (om_a, om_1)."""
+        """Residual + preconditioner + outer update in one clustered kernel (adrt_outer_step, or adrt_outer_step_ff
+        when x_new is a float-float state (B, 2, N, N)); om_img (device (B, 2) FP64, optional): per-image
+        (om_a, om_1)."""
         p = self.plan
         pc = {"none": 0, "g1": 1, "lorr": 2}[p.precond] if p.method == "hybrid" else 0
         if pc == 1:
@@ -480,6 +491,11 @@ class Pipeline:
         else:
             coef = np.zeros(1)
         parts = (self.parts[0], self.parts[1], self.parts[2]) if with_parts else (None, None, None)
+        if x_new.dim() == 4:
+            C.call("adrt_outer_step_ff", p.n, self.B, C.ptr(y), C.ptr(parts[0]), C.ptr(parts[1]), C.ptr(parts[2]),
+                   C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc, p.g1_deg if pc == 1 else 0,
+                   coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), self.band & 0xFF, C.stream_handle())
+            return
         C.call("adrt_outer_step", self.stencil_code, self._codes(), p.n, self.B, C.ptr(y), C.ptr(parts[0]),
                C.ptr(parts[1]), C.ptr(parts[2]), C.ptr(x), C.ptr(x_prev), C.ptr(x_new), om_a, om_1, a0, pc,
                p.g1_deg if pc == 1 else 0, coef.ctypes.data_as(ctypes.c_void_p), C.ptr(om_img), self.band,
@@ -516,6 +532,8 @@ class Pipeline:
         t = self.tables
         bufs = [self.Y, self.parts, self.y, self.s, *self.xs, *self.st, t.roots, t.deg, t.coef, t.rows_main,
                 t.rows_dense, *t._dense_dev.values()]
+        if self.x64 is not None:
+            bufs.append(self.x64)
         if t.high_ff:
             bufs += [t.roots64, t.coef64]
         if t._zd is not None:
@@ -524,6 +542,12 @@ class Pipeline:
             if getattr(self, name, None) is not None:
                 bufs.append(getattr(self, name))
         return sum(x.numel() * x.element_size() for x in bufs)
+
+    @staticmethod
+    def ff_state_for(plan: Plan, precision="fp32", stencil_precision=None):
+        """Whether a pipeline keeps its outer state as float-float planes: where the register-resident fused outer
+        step runs (FP32 rows and stencil, 64 <= N <= 512)."""
+        return precision == "fp32" and (stencil_precision or precision) == "fp32" and 6 <= plan.n <= 9
 
     @staticmethod
     def estimate_bytes(plan: Plan, batch, precision="fp32", stencil_precision=None, captured=True):
@@ -536,7 +560,9 @@ class Pipeline:
         nd = 2 * len(plan.dense_freqs)
         ff = getattr(plan, "high_rows", "dense") == "ff" and nd > 0
         img = B * N * N
-        total = B * 2 * L * N * 2 * rs + 3 * img * rs + 4 * img * 8 + 4 * img * ss
+        # y and three outer states: FP64, or FP32 y, float-float states and the FP64 result buffer
+        state = 36 * img if Pipeline.ff_state_for(plan, precision, stencil_precision) else 32 * img
+        total = B * 2 * L * N * 2 * rs + 3 * img * rs + state + 4 * img * ss
         if ff:  # FP64 roots and coefficients of the compensated rows instead of dense operators
             total += L * 16 + plan.coef.size * 8
         else:
@@ -666,14 +692,31 @@ class Pipeline:
             if xp is not None:
                 free.append(xp)
             xp, x = x, xn
-        return x
+        return self.result(x)
+
+    def result(self, x, out=None):
+        """The FP64 images of an outer state: x itself (FP64 state), or hi + lo of float-float planes converted into
+        out (default: this pipeline's result buffer, rows matching x's)."""
+        if x.dim() == 3:
+            return x
+        if out is None:
+            out = self.x64[:x.shape[0]]
+        C.call("adrt_ff_to_f64", self.plan.n, x.shape[0], C.ptr(x), C.ptr(out), C.stream_handle())
+        return out
 
     # ---------------------------------------------------------------- the stages around the row engine
     def pack(self, src, sino):
-        """The pack + FFT kernel of one packed pass: sinograms (B, 4, 2N-1, N) or images (B, N, N) -> Y."""
+        """The pack + FFT kernel of one packed pass: sinograms (B, 4, 2N-1, N), images (B, N, N) or float-float
+        images (B, 2, N, N) -> Y. Of a float-float image only the hi plane is read: the FFT runs in FP32, and the
+        FP32 rounding of hi + lo is hi."""
         p, st = self.plan, C.stream_handle()
+        stride = 0
+        if not sino and src.dim() == 4:
+            if src.shape[1] != 2 or src.dtype != torch.float32 or not src.is_contiguous():
+                raise ValueError("float-float images are contiguous (B, 2, N, N) FP32")
+            stride = 2 * p.N * p.N
         C.call("adrt_pack_fft", self._codes(), p.n, self.B, 1 if sino else 0, C.dtype_code(src.dtype), C.ptr(src),
-               C.ptr(self.Y), C.ptr(self.tables.roots), self.fft_cols, st)
+               stride, C.ptr(self.Y), C.ptr(self.tables.roots), self.fft_cols, st)
 
     def finish_pass(self, ops):
         """Everything of a packed pass after the polynomial-row launch: the dense (or compensated) rows, the inverse

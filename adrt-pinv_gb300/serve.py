@@ -265,7 +265,8 @@ class SlotLane:
                     continue
                 self.hk[i] += 1
                 if self.hk[i] == self.D:
-                    self.stage_out[i].copy_(new[i], non_blocking=True)
+                    res = self.pipe.result(new[i:i + 1], None if self.pipe.x64 is None else self.pipe.x64[i:i + 1])
+                    self.stage_out[i].copy_(res[0], non_blocking=True)
                     ev = torch.cuda.Event()
                     ev.record(self.stream)
                     self.out_events.append((i, r, ev))

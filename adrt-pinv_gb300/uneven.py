@@ -198,7 +198,7 @@ class PersistentUnevenBatch:
             self._fork(cap, act, pack_g)
             self._rows(("G", act), cap)
             self._fork(cap, act, finish_g)
-        return [state[i][0] for i in range(len(self.pipes))]
+        return [self.pipes[i].result(state[i][0]) for i in range(len(self.pipes))]
 
     def set_inputs(self, sinos):
         for dst, src in zip(self.inputs, sinos):

@@ -141,9 +141,10 @@ int adrt_cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* ou
  * pairs (0,1), (2,3) of quadrant strips s_qa + i s_qb are transformed with a length L = 2N DFT along axis 0 into
  * Y (nimg x 2L x N complex, dtype). src_kind 0: src is nimg images N x N (real, src_dtype), strips = Tq(q, E x)
  * (fastspec.py:142-152); src_kind 1: src is nimg sinograms 4 x (2N-1) x N, strips = iota(b_q) (fastspec.py:170-174).
- * roots: L roots of unity in dtype. */
-int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, void* Y, const void* roots,
-                  int cols, void* stream);
+ * roots: L roots of unity in dtype. src_stride (src_kind 0): elements from one image to the next (0: N*N; e.g.
+ * 2 N*N to read the hi planes of float-float images). cols: strip columns per CTA (0: the default). */
+int adrt_pack_fft(int dtype, int n, int nimg, int src_kind, int src_dtype, const void* src, long long src_stride,
+                  void* Y, const void* roots, int cols, void* stream);
 
 /* Inverse FFT along the offset axis + unpacking (fastops.py:216-220): from Z (nimg x 2L x N complex) produce the
  * three image-space partial sums whose total is E^T sum_q T_q^T Re/Im(ifft Z) (fastspec.py:154-168):
@@ -188,6 +189,17 @@ int adrt_outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y
                     double a0, int precond, int g1_deg, const double* g1_coef, const double* om_img, int band,
                     void* stream);
 int adrt_outer_step_max_n(int dtype);
+
+/* The fused outer step with a float-float outer state (FP32 stencil and partial images, 64 <= N <= 512): y is FP32
+ * (nimg x N x N); x, x_prev and x_new hold per image an FP32 hi plane then an FP32 lo plane (nimg x 2 x N x N,
+ * value = hi + lo, about 48 significant bits). The residual is y - (p0 + p1 + p2) in FP32 (the value the FP64 form
+ * computes when y is an FP32 sum), the update adds om_a r + om_1 (x - x_prev) with an exact two-sum, and no FP64
+ * arithmetic runs. Other arguments as adrt_outer_step. */
+int adrt_outer_step_ff(int n, int nimg, const float* y, const float* p0, const float* p1, const float* p2,
+                       const float* x, const float* x_prev, float* x_new, double om_a, double om_1, double a0,
+                       int precond, int g1_deg, const double* g1_coef, const double* om_img, int band, void* stream);
+/* float-float planes (nimg x 2 x N x N) to FP64 (nimg x N x N). */
+int adrt_ff_to_f64(int n, int nimg, const float* x, double* out, void* stream);
 
 /* Dense low-frequency rows (fastops.py:28-40, 100-117): for r < nrows and every image b,
  *   Y[b, rows[r], :] <- W_r Y[b, rows[r], :]     (W: nrows x N x N complex, row-major, dtype; Y rows of N complex at

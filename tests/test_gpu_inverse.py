@@ -231,6 +231,83 @@ def test_register_outer_step_matches_shared_form(pkg, n, nimg, band, precond):
             assert rel_err(got[i], 0.5 * O.g1_inv(yh[i])) < 1e-5
 
 
+def _ff_planes(v):
+    """FP64 images (B, N, N) -> float-float planes (B, 2, N, N): hi = fl32(v), lo = fl32(v - hi)."""
+    import torch
+
+    hi = v.float()
+    return torch.stack([hi, (v - hi.double()).float()], 1).contiguous()
+
+
+@pytest.mark.parametrize("n,nimg,precond,per_image", [(6, 3, "g1", False), (8, 5, "g1", True), (8, 40, "lorr", False),
+                                                      (9, 2, "g1", False), (7, 4, "none", True)])
+def test_float_float_state_outer_step(pkg, n, nimg, precond, per_image):
+    """adrt_outer_step_ff (outer state as float-float planes, FP32 y, FP32 arithmetic only) against the FP64-state
+    fused step on the same values. The residual and the preconditioner are the same FP32 computation (y - sum of
+    the parts rounds once either way), so the new states differ only by the FP32 rounding of the update
+    om_a r + om_1 (x - x_prev): within 1e-6 of the update. The first step a0 P(y) is a float-float product (1e-12)."""
+    import torch
+
+    N = 1 << n
+    method = "lp" if precond == "none" else "hybrid"
+    plan = pkg.Plan(method, n, np.full(2 * N, 4.0), precond="g1" if precond == "none" else precond, outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, nimg, "fp32")
+    assert pipe.ff_state and pipe.fused_outer_ok()
+    g = torch.Generator(device="cuda").manual_seed(n + nimg)
+    y32 = torch.randn((nimg, N, N), dtype=torch.float32, device="cuda", generator=g)
+    pipe.parts.normal_(generator=g)
+    x = torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    xp = x + 0.1 * torch.randn((nimg, N, N), dtype=torch.float64, device="cuda", generator=g)
+    om = torch.rand((nimg, 2), dtype=torch.float64, device="cuda", generator=g) if per_image else None
+    out64 = torch.empty_like(x)
+    outff = torch.empty((nimg, 2, N, N), dtype=torch.float32, device="cuda")
+    pipe.fused_outer_step(y32.double(), True, x, xp, out64, 0.7, 0.3, 0.0, om_img=om)
+    pipe.fused_outer_step(y32, True, _ff_planes(x), _ff_planes(xp), outff, 0.7, 0.3, 0.0, om_img=om)
+    got = pipe.result(outff, torch.empty_like(x))
+    assert ((got - out64).abs().max() / (out64 - x).abs().max()).item() < 1e-6
+    pipe.fused_outer_step(y32.double(), False, None, None, out64, 0.0, 0.0, 0.37)
+    pipe.fused_outer_step(y32, False, None, None, outff, 0.0, 0.0, 0.37)
+    got = pipe.result(outff, torch.empty_like(x))
+    assert ((got - out64).abs().max() / out64.abs().max()).item() < 1e-12
+    # the float-float result keeps hi = fl32(hi + lo): its planes are normalised
+    assert torch.equal(outff[:, 0], (outff[:, 0].double() + outff[:, 1].double()).float())
+
+
+def test_pack_reads_hi_plane_of_float_float_images(pkg):
+    """The pack of float-float images (B, 2, N, N) reads the hi planes (image stride 2 N^2): the same packed rows as
+    the pack of the hi planes alone."""
+    import torch
+
+    n, B = 7, 3
+    N = 1 << n
+    plan = pkg.Plan("hybrid", n, np.full(2 * N, 4.0), outer=(1.0, 2.0, 3))
+    pipe = pkg.Pipeline(plan, B, "fp32")
+    x = torch.randn((B, 2, N, N), dtype=torch.float32, device="cuda")
+    pipe.pack(x, sino=False)
+    y1 = pipe.Y.clone()
+    pipe.pack(x[:, 0].contiguous(), sino=False)
+    assert torch.equal(y1, pipe.Y)
+
+
+def test_float_float_state_inverse_matches_fp64_state(pkg, hybrid256):
+    """The whole N=256 hybrid inverse with the float-float outer state (the default) against the same pipeline with
+    the FP64 outer state: both compute the rows, FFTs and stencil in FP32, so they agree far inside the 1e-5
+    accuracy target (1e-6)."""
+    import torch
+
+    n, N, B = 8, 256, 4
+    bs = np.stack([pkg.phantoms.add_noise(pkg.adrtcore.adrt(n, pkg.phantoms.ellipse_phantom(N, seed=s)), 1e-3, seed=s + 50)
+                   for s in range(B)])
+    bd = torch.from_numpy(bs).cuda()
+    pa = pkg.Pipeline(hybrid256.plan, B, "fp32")
+    pb = pkg.Pipeline(hybrid256.plan, B, "fp32", state="fp64")
+    assert pa.ff_state and not pb.ff_state
+    xa = pa.apply(bd).clone()
+    xb = pb.apply(bd)
+    for i in range(B):
+        assert rel_err(xa[i].cpu().numpy(), xb[i].cpu().numpy()) < 1e-6
+
+
 @pytest.mark.parametrize("sprec,tol", [("fp64", 1e-12), ("ff", 1e-10)])
 @pytest.mark.parametrize("n,nimg", [(4, 2), (6, 3), (8, 3), (8, 40)])
 def test_fused_cross_quadrant_inverse_high_precision(pkg, sprec, tol, n, nimg):

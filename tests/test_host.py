@@ -72,7 +72,7 @@ def test_argument_validation_without_gpu(lib):
     assert lib.cheb_rows(12, 4, p(z), p(deg), p(a), p(a), 1.0, p(X), p(X), 1, 3, 1, None) == 1
     assert lib.cert_rowsum(0, 4, p(a), 1, p(a), 1) == 1
     assert lib.adrt_rows_run(None, None) == 1
-    assert lib.adrt_pack_fft(0, 12, 1, 0, 0, None, None, None, 0, None) == 1
+    assert lib.adrt_pack_fft(0, 12, 1, 0, 0, None, 0, None, None, 0, None) == 1
     assert lib.adrt_ifft_unpack(0, 3, 1, None, None, None, None, None, 0, None) == 1
     assert lib.adrt_forward(0, 0, 1, None, None, None, None) == 1
     assert lib.adrt_outer_update(0, 3, 1, None, None, None, 1, None, 0.0, 0.0, 0.0, None, None) == 1  # f64 r, f32 x
