@@ -95,6 +95,7 @@ PROTOTYPES = {
     "adrt_outer_step_ff": [_I, _I, _P, _P, _P, _P, _P, _P, _P, _D, _D, _D, _I, _I, _P, _P, _I, _P],
     "adrt_ff_to_f64": [_I, _I, _P, _P, _P],
     "adrt_dense_rows": [_I, _I, _I, _I, _P, _P, _P, ctypes.c_longlong, _P, _P, _I, _I, _P],
+    "adrt_dense_split": [_I, _I, _P, _P, _P],
     "adrt_forward": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_transpose": [_I, _I, _I, _P, _P, _P, _P],
     "adrt_cgls_start": [ctypes.POINTER(CglsState), _P, _P],

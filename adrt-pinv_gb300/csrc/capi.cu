@@ -297,6 +297,10 @@ int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, 
     return dense_rows(dtype, n, nimg, nrows, rows, W, Y, img_stride, Zd, err, use_tc, tile, as_stream(stream));
 }
 
+int adrt_dense_split(int n, int nrows, const void* W, void* Ws, void* stream) {
+    return dense_split(n, nrows, W, Ws, as_stream(stream));
+}
+
 int adrt_forward(int dtype, int n, int nimg, const void* x, void* b, void* scratch, void* stream) {
     return adrt_fwd(dtype, n, nimg, x, b, scratch, as_stream(stream));
 }

@@ -358,6 +358,290 @@ __global__ void __launch_bounds__(TC_THREADS) dense_tc_kernel(int N, int nimg, c
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
 }
 
+// ------------------------------------------------------------------ complex-blocked tensor-core kernel on pre-split
+// operators (N >= 128, FP32 data). The operators are constant, so they are split once (dense_split) into TF32 tiles in
+// the MMA's K-major layout: per (dense row, block of 128 output rows, chunk of 16 input columns) four 8 KB tiles
+// Re W hi, Re W lo, Im W hi, Im W lo, stored contiguously (32 KB per chunk, one bulk copy). With the images' rows split
+// the same way per chunk, three TMEM accumulators hold
+//     P1 = Re W Re y,   P2 = Im W Im y,   P3 = Im W Re y + Re W Im y     (each term 3xTF32: hi hi + hi lo + lo hi)
+// and z = (P1 - P2) + i P3: half the operator bytes of the real 2N x 2N form for the same products. Pipeline: a ring
+// of CX_S stages; one thread issues the bulk copy of a chunk's operator tiles two chunks ahead (mbarrier with a byte
+// count), every thread converts its share of the image rows of the current chunk into the stage, one thread issues
+// the chunk's 24 MMAs into one of two accumulator sets and commits them to the stage's mbarrier, and the chunk two
+// back is folded into FP32 registers (its MMAs complete by then) while the tensor cores run the current one.
+constexpr int CX_M = 128;            // complex output rows per CTA (TMEM lanes)
+constexpr int CX_KC = 16;            // complex input columns per chunk
+constexpr int CX_S = 4;              // pipeline stages
+constexpr int CX_TILE = CX_M * CX_KC;  // floats per operator tile
+constexpr int CX_THREADS = 256;
+
+// W (nrows x N x N complex FP32, [row][out][in]) -> Ws (nrows x N/128 x N/16 x 4 tiles x CX_TILE floats); element
+// (o, i) of a tile at float ((o%128)/8 * (CX_KC/4) + (i%16)/4) * 32 + (o%8) * 4 + i%4 (core matrices of 8 rows x 16 B)
+__global__ void dense_split_kernel(int N, long long total, const float2* __restrict__ W, float* __restrict__ Ws) {
+    const int MT = N / CX_M, NC = N / CX_KC;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total; e += (long long)gridDim.x * blockDim.x) {
+        const long long ro = e / N;
+        const int i = (int)(e - ro * N);
+        const long long r = ro / N;
+        const int o = (int)(ro - r * N);
+        const float2 w = W[e];
+        const int mt = o / CX_M, om = o % CX_M, c = i / CX_KC, k = i % CX_KC;
+        float* t = Ws + (((size_t)r * MT + mt) * NC + c) * 4 * CX_TILE + ((om / 8) * (CX_KC / 4) + k / 4) * 32 +
+                   (om % 8) * 4 + (k % 4);
+        const uint32_t reh = to_tf32(w.x), imh = to_tf32(w.y);
+        t[0] = __uint_as_float(reh);
+        t[CX_TILE] = __uint_as_float(to_tf32(w.x - __uint_as_float(reh)));
+        t[2 * CX_TILE] = __uint_as_float(imh);
+        t[3 * CX_TILE] = __uint_as_float(to_tf32(w.y - __uint_as_float(imh)));
+    }
+}
+
+__device__ __forceinline__ void mbar_expect_bulk(uint32_t mbar, uint32_t dst, const void* src, uint32_t bytes) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}\n" ::"r"(mbar),
+                 "r"(bytes)
+                 : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(mbar)
+                 : "memory");
+}
+
+template <int BP>
+__global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg, const int* __restrict__ rows,
+                                                                 const float* __restrict__ Ws,
+                                                                 const float2* __restrict__ Y, long long img_stride,
+                                                                 float2* __restrict__ Zd, int* __restrict__ err) {
+    constexpr int A_BYTES = 4 * CX_TILE * 4;  // 32 KB
+    constexpr int XT = BP * CX_KC;            // floats per image tile
+    constexpr int STAGE = A_BYTES + 4 * XT * 4;
+    constexpr int NACC = 3 * BP;  // columns of one accumulator set (P1, P2, P3)
+    constexpr int NCOLS = 2 * NACC <= 128 ? 128 : (2 * NACC <= 256 ? 256 : 512);
+    constexpr int HB = BP / 2;  // image columns folded per warp
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + CX_S * STAGE);  // operator tiles of the stage landed
+    uint64_t* done = full + CX_S;                                           // MMAs reading the stage completed
+    uint64_t* drain = done + CX_S;
+    uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
+    int* s_fail = reinterpret_cast<int*>(tmem_slot + 1);  // set by the MMA thread when operator tiles did not land
+
+    const int r = blockIdx.x, mt = blockIdx.y, b0 = blockIdx.z * BP;
+    const int MT = N / CX_M, NC = N / CX_KC;
+    const float* Wr = Ws + ((size_t)r * MT + mt) * NC * 4 * CX_TILE;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long yrow = (long long)rows[r] * N;
+
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
+                     "r"(NCOLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (threadIdx.x == 0) {
+        for (int q = 0; q < 2 * CX_S + 1; ++q)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        *s_fail = 0;
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    const uint32_t tmem = *tmem_slot;
+
+    // instruction descriptor: D f32, A and B tf32, both K-major, N = BP, M = 128
+    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BP >> 3) << 17) | ((uint32_t)(CX_M >> 4) << 24);
+    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+    const int col0 = (warp >> 2) * HB;
+    float zr[HB], zi[HB];
+#pragma unroll
+    for (int q = 0; q < HB; ++q) zr[q] = zi[q] = 0.f;
+    bool ok = true;
+    int issued = 0, consumed = 0;  // operator chunks whose bulk copy was issued / seen landed (thread 0)
+
+    // fold accumulator set s (one chunk's partial sums) into zr, zi
+    auto promote = [&](int s) {
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t base = tmem + lane_base + (uint32_t)(s * NACC + col0);
+#pragma unroll
+        for (int c = 0; c < HB; c += 8) {
+            uint32_t p1[8], p2[8], p3[8];
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(p1[0]), "=r"(p1[1]), "=r"(p1[2]), "=r"(p1[3]), "=r"(p1[4]), "=r"(p1[5]), "=r"(p1[6]),
+                           "=r"(p1[7])
+                         : "r"(base + c));
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(p2[0]), "=r"(p2[1]), "=r"(p2[2]), "=r"(p2[3]), "=r"(p2[4]), "=r"(p2[5]), "=r"(p2[6]),
+                           "=r"(p2[7])
+                         : "r"(base + BP + c));
+            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                         : "=r"(p3[0]), "=r"(p3[1]), "=r"(p3[2]), "=r"(p3[3]), "=r"(p3[4]), "=r"(p3[5]), "=r"(p3[6]),
+                           "=r"(p3[7])
+                         : "r"(base + 2 * BP + c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                zr[c + q] += __uint_as_float(p1[q]) - __uint_as_float(p2[q]);
+                zi[c + q] += __uint_as_float(p3[q]);
+            }
+        }
+    };
+    auto issue_a = [&](int kc) {  // thread 0: the operator tiles of chunk kc into stage kc % CX_S
+        const int s = kc % CX_S;
+        mbar_expect_bulk(smem_addr(&full[s]), smem_addr(smem_raw + s * STAGE), Wr + (size_t)kc * 4 * CX_TILE, A_BYTES);
+    };
+
+    // image rows: thread t loads 4 consecutive complex values (t % 4: which quad of the chunk) of image t / 4
+    constexpr int XTHREADS = BP * (CX_KC / 4);
+    const int xb = threadIdx.x / (CX_KC / 4), xq = threadIdx.x % (CX_KC / 4);
+    const bool xon = threadIdx.x < XTHREADS;
+    const bool xlive = xon && b0 + xb < nimg;
+    const float4* ysrc = reinterpret_cast<const float4*>(Y + (long long)(b0 + xb) * img_stride + yrow + 4 * xq);
+    float4 ya = make_float4(0.f, 0.f, 0.f, 0.f), yb = ya;
+    auto load_x = [&](int kc) {
+        if (xlive) {
+            ya = ysrc[kc * (CX_KC / 2)];
+            yb = ysrc[kc * (CX_KC / 2) + 1];
+        }
+    };
+    if (threadIdx.x == 0) {
+        for (int kc = 0; kc < 2 && kc < NC; ++kc) issue_a(kc);
+        issued = NC < 2 ? NC : 2;
+    }
+    load_x(0);
+
+    for (int kc = 0; kc < NC; ++kc) {
+        const int s = kc % CX_S;
+        unsigned char* st = smem_raw + s * STAGE;
+        if (kc >= 2) {
+            // chunk kc-2: its MMAs read stage (kc+2) % CX_S and wrote accumulator set kc % 2
+            const int w = mbar_wait(smem_addr(&done[(kc - 2) % CX_S]), (uint32_t)(((kc - 2) / CX_S) & 1)) ? 1 : 0;
+            ok = __syncthreads_and(w && !*s_fail) != 0;
+            if (!ok) break;
+            promote(kc & 1);
+        }
+        if (threadIdx.x == 0 && kc + 2 < NC) {
+            issue_a(kc + 2);
+            issued = kc + 3;
+        }
+        if (xon) {  // the image tiles of chunk kc: Re hi, Re lo, Im hi, Im lo
+            const float re[4] = {ya.x, ya.z, yb.x, yb.z}, im[4] = {ya.y, ya.w, yb.y, yb.w};
+            uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                rh[q] = to_tf32(re[q]);
+                rl[q] = to_tf32(re[q] - __uint_as_float(rh[q]));
+                ih[q] = to_tf32(im[q]);
+                il[q] = to_tf32(im[q] - __uint_as_float(ih[q]));
+            }
+            const int off = ((xb / 8) * (CX_KC / 4) + xq) * 128 + (xb % 8) * 16;
+            unsigned char* xt = st + A_BYTES;
+            *reinterpret_cast<uint4*>(xt + off) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+            *reinterpret_cast<uint4*>(xt + XT * 4 + off) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+            *reinterpret_cast<uint4*>(xt + 2 * XT * 4 + off) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+            *reinterpret_cast<uint4*>(xt + 3 * XT * 4 + off) = make_uint4(il[0], il[1], il[2], il[3]);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        __syncthreads();
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        if (threadIdx.x == 0) {
+            const bool landed = !*s_fail && mbar_wait(smem_addr(&full[s]), (uint32_t)((kc / CX_S) & 1));
+            if (landed) {
+                consumed = kc + 1;
+                const uint32_t d = tmem + (uint32_t)((kc & 1) * NACC);
+                const uint32_t a0 = smem_addr(st), x0 = smem_addr(st + A_BYTES);
+                constexpr uint32_t SBO = (CX_KC / 4) * 128;
+#pragma unroll
+                for (int k8 = 0; k8 < CX_KC / 8; ++k8) {
+                    const uint32_t ko = k8 * 256;
+                    const uint64_t reh = desc_kmajor(a0 + ko, 128, SBO), rel = desc_kmajor(a0 + CX_TILE * 4 + ko, 128, SBO);
+                    const uint64_t imh = desc_kmajor(a0 + 2 * CX_TILE * 4 + ko, 128, SBO);
+                    const uint64_t iml = desc_kmajor(a0 + 3 * CX_TILE * 4 + ko, 128, SBO);
+                    const uint64_t xrh = desc_kmajor(x0 + ko, 128, SBO), xrl = desc_kmajor(x0 + XT * 4 + ko, 128, SBO);
+                    const uint64_t xih = desc_kmajor(x0 + 2 * XT * 4 + ko, 128, SBO);
+                    const uint64_t xil = desc_kmajor(x0 + 3 * XT * 4 + ko, 128, SBO);
+                    const uint32_t fresh = k8 > 0 ? 1u : 0u;
+                    mma_tf32(d, reh, xrh, idesc, fresh);  // P1 = Re W Re y
+                    mma_tf32(d, reh, xrl, idesc, 1u);
+                    mma_tf32(d, rel, xrh, idesc, 1u);
+                    mma_tf32(d + BP, imh, xih, idesc, fresh);  // P2 = Im W Im y
+                    mma_tf32(d + BP, imh, xil, idesc, 1u);
+                    mma_tf32(d + BP, iml, xih, idesc, 1u);
+                    mma_tf32(d + 2 * BP, imh, xrh, idesc, fresh);  // P3 = Im W Re y + Re W Im y
+                    mma_tf32(d + 2 * BP, imh, xrl, idesc, 1u);
+                    mma_tf32(d + 2 * BP, iml, xrh, idesc, 1u);
+                    mma_tf32(d + 2 * BP, reh, xih, idesc, 1u);
+                    mma_tf32(d + 2 * BP, reh, xil, idesc, 1u);
+                    mma_tf32(d + 2 * BP, rel, xih, idesc, 1u);
+                }
+            }
+            // commit even when the tiles did not land (no MMA issued then), so the done barriers keep their phases;
+            // the flag stops every thread at its next check
+            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                             smem_addr(&done[s]))
+                         : "memory");
+            if (!landed) *s_fail = 1;
+        }
+        if (kc + 1 < NC) load_x(kc + 1);
+    }
+    if (ok) {  // the last two chunks
+        for (int kc = NC - 2 > 0 ? NC - 2 : 0; kc < NC; ++kc) {
+            const int w = mbar_wait(smem_addr(&done[kc % CX_S]), (uint32_t)((kc / CX_S) & 1)) ? 1 : 0;
+            ok = __syncthreads_and(w && !*s_fail) != 0;
+            if (!ok) break;
+            promote(kc & 1);
+        }
+    }
+    if (!ok && threadIdx.x == 0) {
+        // a wait gave up: before the tensor memory is freed and the CTA leaves, every MMA it issued (one more commit
+        // to the spare barrier) and every operator copy it issued (the stages' byte counts) must have completed;
+        // both waits are bounded. Flag 1: this launch's dense rows were not written; 2: even the drain ran out.
+        asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                         smem_addr(drain))
+                     : "memory");
+        bool drained = mbar_wait(smem_addr(drain), 0u);
+        for (int kc = consumed; kc < issued; ++kc)  // at most three outstanding copies, in distinct stages
+            drained = mbar_wait(smem_addr(&full[kc % CX_S]), (uint32_t)((kc / CX_S) & 1)) && drained;
+        atomicMax(err, drained ? 1 : 2);
+    }
+    if (ok) {
+        const int o = mt * CX_M + (warp & 3) * 32 + lane;
+#pragma unroll
+        for (int q = 0; q < HB; ++q) {
+            const int b = b0 + col0 + q;
+            if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = make_float2(zr[q], zi[q]);
+        }
+    }
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
+}
+
+template <int BP>
+static int launch_cx(int n, int nimg, int nrows, const int* rows, const void* Ws, const void* Y, long long img_stride,
+                     void* Zd, int* err, cudaStream_t st) {
+    const int N = 1 << n;
+    const size_t smem = (size_t)CX_S * (4 * CX_TILE * 4 + 4 * BP * CX_KC * 4) + 128;  // stages, barriers, slots
+    auto kern = dense_cx_kernel<BP>;
+    if (int rc = ensure_smem((const void*)kern, smem)) return rc;
+    dim3 grid(nrows, N / CX_M, (nimg + BP - 1) / BP);
+    kern<<<grid, CX_THREADS, smem, st>>>(N, nimg, rows, reinterpret_cast<const float*>(Ws),
+                                         reinterpret_cast<const float2*>(Y), img_stride, reinterpret_cast<float2*>(Zd),
+                                         err);
+    return launch_status("dense_cx_kernel");
+}
+
+int dense_split(int n, int nrows, const void* W, void* Ws, cudaStream_t st) {
+    if (n < 7 || n > 10 || nrows < 0 || (nrows && (!W || !Ws))) {
+        set_error("dense_split: bad arguments (n=%d nrows=%d; n must be 7..10)", n, nrows);
+        return ADRT_EINVAL;
+    }
+    const long long total = (long long)nrows << (2 * n);
+    if (!total) return ADRT_OK;
+    long long g = (total + 255) / 256;
+    if (g > 65535LL * 16) g = 65535LL * 16;
+    dense_split_kernel<<<(int)g, 256, 0, st>>>(1 << n, total, reinterpret_cast<const float2*>(W),
+                                               reinterpret_cast<float*>(Ws));
+    return launch_status("dense_split_kernel");
+}
+
 template <int BP>
 static int launch_tc(int n, int nimg, int nrows, const int* rows, const void* W, const void* Y, long long img_stride,
                      void* Zd, int* err, cudaStream_t st) {
@@ -385,7 +669,17 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
     if (!nimg || !nrows) return ADRT_OK;
     const int N = 1 << n;
     int rc;
-    if (use_tc == 2) {
+    if (use_tc == 3) {
+        if (dtype != ADRT_F32 || n < 7 || n > 10 || !err) {
+            set_error("dense_rows: the pre-split tensor-core kernel (use_tc = 3) takes FP32, 7 <= n <= 10 and an error "
+                      "flag");
+            return ADRT_EINVAL;
+        }
+        const int bp = tile ? tile : (nimg <= 16 ? 16 : (nimg <= 32 ? 32 : 64));
+        if (bp == 16) rc = launch_cx<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        else if (bp == 32) rc = launch_cx<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        else rc = launch_cx<64>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+    } else if (use_tc == 2) {
         if (dtype != ADRT_F32 || nimg > 16) {
             set_error("dense_rows: the streaming kernel (use_tc = 2) takes FP32 and at most 16 images (nimg=%d)", nimg);
             return ADRT_EINVAL;

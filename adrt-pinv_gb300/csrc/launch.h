@@ -38,5 +38,6 @@ int outer_step_ff(int n, int nimg, const float* y, const float* p0, const float*
 int ff_to_f64(int n, int nimg, const float* x, double* out, cudaStream_t st);
 int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const void* W, void* Y, long long img_stride,
                void* Zd, int* err, int use_tc, int tile, cudaStream_t st);
+int dense_split(int n, int nrows, const void* W, void* Ws, cudaStream_t st);
 int cert_rowsum_dev(int n, int K, const double* omega, int m_lo, double* out, cudaStream_t st);
 }  // namespace adrt

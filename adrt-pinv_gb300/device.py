@@ -61,6 +61,7 @@ class RowTables:
         self.count = 0  # level-rows applied, counted as the reference does
         self.timer = None  # list: when set, (start, end) CUDA events of every polynomial-row launch are appended
         self.use_tc = real == torch.float32  # dense rows on tensor cores in FP32
+        self.split_dense = True  # the tensor-core rows on pre-split operators where the kernel exists (dense_mode)
         # small batches (<= 16 images, FP32): the streaming CUDA-core kernel, with the operators stored transposed;
         # set by the owning pipeline before the first dense table is built
         self.stream_dense = False
@@ -164,6 +165,26 @@ class RowTables:
             raise RuntimeError("dense_tc_kernel: an mbarrier wait ran out; the dense-row results of that launch "
                                "were not written" + more)
 
+    def split_table(self, T):
+        """The pre-split form of a dense table T for the complex-blocked tensor-core kernel (adrt_dense_split),
+        built once per table and shared like the table itself."""
+        Ws = getattr(T, "_adrt_split", None)  # held by the table itself: it lives exactly as long as T
+        if Ws is None:
+            N = self.plan.N
+            Ws = torch.empty((T.shape[0], 4 * N * N), dtype=torch.float32, device=self.device)
+            C.call("adrt_dense_split", self.plan.n, T.shape[0], C.ptr(T), C.ptr(Ws), C.stream_handle())
+            T._adrt_split = Ws
+        return Ws
+
+    def dense_mode(self):
+        """Kernel of the dense rows: 3 complex-blocked tensor cores on pre-split operators (FP32, 7 <= n <= 10),
+        1 the real-form tensor-core kernel, 2 the streaming CUDA-core kernel (small FP32 batches), 0 CUDA cores."""
+        if self.stream_dense:
+            return 2
+        if not self.use_tc:
+            return 0
+        return 3 if self.split_dense and 7 <= self.plan.n <= 10 else 1
+
     def dense_apply(self, Y, T):
         """Y[b, r] <- T_r Y[b, r] for the dense rows (FP32: tensor cores, or the streaming CUDA-core kernel for small
         batches; FP64: CUDA cores)."""
@@ -171,9 +192,10 @@ class RowTables:
         nd = int(self.rows_dense.numel())
         if self._zd is None or self._zd.shape[1] != B:
             self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
-        mode = 2 if self.stream_dense else (1 if self.use_tc else 0)
-        C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(T), C.ptr(Y), R * N,
-               C.ptr(self._zd), C.ptr(self.err), mode, self.dense_tile if mode == 1 else 0, C.stream_handle())
+        mode = self.dense_mode()
+        W = self.split_table(T) if mode == 3 else T
+        C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(W), C.ptr(Y), R * N,
+               C.ptr(self._zd), C.ptr(self.err), mode, self.dense_tile if mode in (1, 3) else 0, C.stream_handle())
 
     def run_ff(self, Y, ops):
         """The op list on the high-condition rows in float-float arithmetic (adrt_rows_ff_run)."""
@@ -390,7 +412,7 @@ class Pipeline:
         q.__dict__.update(self.__dict__)
         q.B = b
         t = RowTables(self.plan, self.real, self.device)
-        for k in ("stream_dense", "use_tc", "row_grid", "dense_tile"):
+        for k in ("stream_dense", "use_tc", "split_dense", "row_grid", "dense_tile"):
             setattr(t, k, getattr(self.tables, k))
         q.tables = t
         q.Y = self.Y[:b]
@@ -534,6 +556,7 @@ class Pipeline:
                 t.rows_dense, *t._dense_dev.values()]
         if self.x64 is not None:
             bufs.append(self.x64)
+        bufs += [T._adrt_split for T in t._dense_dev.values() if getattr(T, "_adrt_split", None) is not None]
         if t.high_ff:
             bufs += [t.roots64, t.coef64]
         if t._zd is not None:
@@ -567,6 +590,8 @@ class Pipeline:
             total += L * 16 + plan.coef.size * 8
         else:
             total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
+            if precision == "fp32" and B > 16 and 7 <= plan.n <= 10:  # their pre-split tensor-core form
+                total += 2 * nd * N * N * 16
         total += L * 2 * rs + 3 * L * 4 + plan.coef.size * rs  # roots; deg and the row lists; coefficients
         if captured:  # the two input buffers of the captured graphs
             total += 2 * B * 4 * (2 * N - 1) * N * 8

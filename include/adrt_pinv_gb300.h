@@ -207,10 +207,16 @@ int adrt_ff_to_f64(int n, int nimg, const float* x, double* out, void* stream);
  * copied back. use_tc = 1 with FP32 and n >= 6: tensor cores (tcgen05.mma kind::tf32, 3xTF32 split, FP32 accumulate);
  * *err (device int) is set to 1 if a tensor-core completion wait ran out. use_tc = 2 (FP32, nimg <= 16): W is given
  * TRANSPOSED (W[r][i][o] = W_r[o][i]) and a CUDA-core kernel streams it once per group of 8 images (small batches,
- * where the product is bound by reading the operators). Otherwise (use_tc = 0) CUDA cores. tile (tensor cores):
- * images per CTA, 16, 32 or 64 (0: chosen from nimg). */
+ * where the product is bound by reading the operators). use_tc = 3 (FP32, 7 <= n <= 10): W is the pre-split table of
+ * adrt_dense_split and the tensor cores run the complex-blocked product (operator tiles by bulk copy through a
+ * four-stage ring). Otherwise (use_tc = 0) CUDA cores. tile (tensor cores): images per CTA, 16, 32 or 64 (0: chosen
+ * from nimg). */
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
                     long long img_stride, void* Zd, int32_t* err, int use_tc, int tile, void* stream);
+/* The operators W (nrows x N x N complex FP32, row-major) split once for use_tc = 3: Ws holds nrows x N/128 x N/16
+ * chunks of four TF32 tiles (Re hi, Re lo, Im hi, Im lo; 128 output rows x 16 input columns each, in the K-major
+ * core-matrix layout of tcgen05.mma), 16 N^2 bytes per row. 7 <= n <= 10. */
+int adrt_dense_split(int n, int nrows, const void* W, void* Ws, void* stream);
 
 /* Spatial ADRT in the reference's sinogram layout (adrtcore.py:122-137), nimg images, exact for integer dtypes
  * (ADRT_I32, ADRT_I64; sums only), FP32 / FP64 otherwise. scratch: 2 * nimg * 4 * (2N-1) * N elements of dtype.

@@ -46,6 +46,51 @@ def test_dense_rows_tc_and_simt(pkg, n, nimg, nrows):
     assert np.abs(Yd.cpu().numpy() - ref).max() / np.abs(ref).max() < 1e-13
 
 
+@pytest.mark.parametrize("n,nimg,nrows,tile", [(8, 64, 6, 0), (8, 100, 3, 0), (7, 40, 4, 32), (9, 20, 2, 16),
+                                               (8, 64, 5, 64), (10, 33, 1, 0)])
+def test_dense_rows_presplit_complex_blocked(pkg, n, nimg, nrows, tile):
+    """The complex-blocked tensor-core kernel on operators pre-split by adrt_dense_split (use_tc = 3: Re / Im W in
+    TF32 hi + lo, z = (ReW Re y - ImW Im y) + i (ImW Re y + ReW Im y), each product 3xTF32 with per-chunk promotion)
+    against the FP64 product: every output row within 5e-7 (norm-wise), images beyond nimg untouched; partial image
+    tiles (nimg not a multiple of the tile) included."""
+    import torch
+
+    C = pkg._lib
+    C.load()
+    N, R = 1 << n, 12
+    rng = np.random.default_rng(n + nimg)
+    W = (rng.standard_normal((nrows, N, N)) + 1j * rng.standard_normal((nrows, N, N))) / np.sqrt(N)
+    Y = rng.standard_normal((nimg, R, N)) + 1j * rng.standard_normal((nimg, R, N))
+    rows = np.array(sorted(rng.choice(R, nrows, replace=False)), dtype=np.int32)
+    ref = Y.copy()
+    for i, r in enumerate(rows):
+        ref[:, r, :] = Y[:, r, :] @ W[i].T
+    Wd = torch.from_numpy(W).to("cuda", torch.complex64)
+    Ws = torch.empty((nrows, 4 * N * N), dtype=torch.float32, device="cuda")
+    assert C.load().adrt_dense_split(n, nrows, C.ptr(Wd), C.ptr(Ws), C.stream_handle()) == 0
+    Yd = torch.from_numpy(Y).to("cuda", torch.complex64)
+    rd = torch.from_numpy(rows).cuda()
+    Zd = torch.empty((nrows, nimg, N), dtype=torch.complex64, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    C.call("adrt_dense_rows", C.F32, n, nimg, nrows, C.ptr(rd), C.ptr(Ws), C.ptr(Yd), R * N, C.ptr(Zd), C.ptr(err), 3,
+           tile, C.stream_handle())
+    torch.cuda.synchronize()
+    assert int(err.item()) == 0
+    out = Yd.cpu().numpy()
+    for r in range(R):
+        e = np.linalg.norm(out[:, r, :] - ref[:, r, :]) / np.linalg.norm(ref[:, r, :])
+        assert e < 5e-7, (r, e)
+    # the split table: tile element (o, i) of (row, 128-row block, 16-column chunk); hi + lo (two TF32 values, about
+    # 22 significant bits together) reproduces the FP32 entry to 2^-21
+    Wh = Ws.cpu().numpy().reshape(nrows, N // 128, N // 16, 4, 2048).astype(np.float64)
+    o, i = 130 % N, 37
+    t = Wh[0, o // 128, i // 16]
+    off = ((o % 128) // 8 * 4 + (i % 16) // 4) * 32 + (o % 8) * 4 + i % 4
+    w32 = np.complex64(W[0, o, i])
+    assert abs(t[0, off] + t[1, off] - float(w32.real)) <= 2.0 ** -21 * abs(float(w32.real))
+    assert abs(t[2, off] + t[3, off] - float(w32.imag)) <= 2.0 ** -21 * abs(float(w32.imag))
+
+
 @pytest.mark.parametrize("n,nimg,nrows", [(6, 1, 3), (8, 3, 5), (9, 8, 2), (11, 2, 1), (7, 13, 3), (10, 16, 1)])
 def test_dense_rows_streaming_small_batch(pkg, n, nimg, nrows):
     """The small-batch streaming kernel (use_tc = 2, operators transposed, passes of 8 images) against the FP64
