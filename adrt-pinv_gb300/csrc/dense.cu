@@ -374,6 +374,9 @@ constexpr int CX_KC = 16;            // complex input columns per chunk
 constexpr int CX_S = 4;              // pipeline stages
 constexpr int CX_TILE = CX_M * CX_KC;  // floats per operator tile
 constexpr int CX_THREADS = 256;
+// after the stages: 3 CX_S + 5 mbarriers, then the TMEM slot and three flags
+constexpr int CX_BAR_BYTES = 256;
+static_assert((3 * CX_S + 5) * 8 + 4 * 4 <= CX_BAR_BYTES, "barrier area too small");
 
 // W (nrows x N x N complex FP32, [row][out][in]) -> Ws (nrows x N/128 x N/16 x 4 tiles x CX_TILE floats); element
 // (o, i) of a tile at float ((o%128)/8 * (CX_KC/4) + (i%16)/4) * 32 + (o%8) * 4 + i%4 (core matrices of 8 rows x 16 B)
@@ -405,6 +408,34 @@ __device__ __forceinline__ void mbar_expect_bulk(uint32_t mbar, uint32_t dst, co
                  : "memory");
 }
 
+// bounded wait that also gives up when another role of the CTA has set the abort flag
+__device__ __forceinline__ bool mbar_wait_or_abort(uint32_t mbar, uint32_t parity, const volatile int* abort_flag) {
+    for (long it = 0; it < (1L << 24); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(mbar), "r"(parity)
+            : "memory");
+        if (done) return true;
+        if ((it & 255) == 255 && *abort_flag) return false;
+    }
+    return false;
+}
+// the same, polled by lane 0 of a converged warp and broadcast, so that every lane takes the same branch
+__device__ __forceinline__ bool warp_wait(uint32_t mbar, uint32_t parity, const volatile int* abort_flag) {
+    int okv = 0;
+    if ((threadIdx.x & 31) == 0) okv = mbar_wait_or_abort(mbar, parity, abort_flag) ? 1 : 0;
+    return __shfl_sync(0xffffffffu, okv, 0) != 0;
+}
+__device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}\n" ::"r"(mbar) : "memory");
+}
+
+// Warp-specialised: warp 0 (one thread) streams the operator tiles of chunk after chunk into the ring, warps 2-3 build
+// the image tiles, warp 1 (one thread) issues the MMAs, warps 4-7 fold each chunk's accumulator set into FP32
+// registers and write the result. Per stage: a_full (operator bytes landed), x_full (64 image-tile arrivals),
+// stage_free (commit of the chunk's MMAs); per accumulator set: acc_full (commit), acc_free (128 fold arrivals).
 template <int BP>
 __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg, const int* __restrict__ rows,
                                                                  const float* __restrict__ Ws,
@@ -412,16 +443,21 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
                                                                  float2* __restrict__ Zd, int* __restrict__ err) {
     constexpr int A_BYTES = 4 * CX_TILE * 4;  // 32 KB
     constexpr int XT = BP * CX_KC;            // floats per image tile
-    constexpr int STAGE = A_BYTES + 4 * XT * 4;
-    constexpr int NACC = 3 * BP;  // columns of one accumulator set (P1, P2, P3)
-    constexpr int NCOLS = 2 * NACC <= 128 ? 128 : (2 * NACC <= 256 ? 256 : 512);
-    constexpr int HB = BP / 2;  // image columns folded per warp
+    constexpr int STAGE = A_BYTES + 6 * XT * 4;  // image tiles: Re hi, Re lo, Im hi, Im lo, -Im hi, -Im lo
+    constexpr int NACC = 2 * BP;                 // columns of one accumulator set (Re z, Im z)
+    constexpr int NCOLS = 2 * NACC <= 64 ? 64 : (2 * NACC <= 128 ? 128 : 256);
+    constexpr int XW = 64;  // image-tile threads (warps 2-3)
     extern __shared__ __align__(1024) unsigned char smem_raw[];
-    uint64_t* full = reinterpret_cast<uint64_t*>(smem_raw + CX_S * STAGE);  // operator tiles of the stage landed
-    uint64_t* done = full + CX_S;                                           // MMAs reading the stage completed
-    uint64_t* drain = done + CX_S;
+    uint64_t* a_full = reinterpret_cast<uint64_t*>(smem_raw + CX_S * STAGE);
+    uint64_t* x_full = a_full + CX_S;
+    uint64_t* stage_free = x_full + CX_S;
+    uint64_t* acc_full = stage_free + CX_S;
+    uint64_t* acc_free = acc_full + 2;
+    uint64_t* drain = acc_free + 2;
     uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(drain + 1);
-    int* s_fail = reinterpret_cast<int*>(tmem_slot + 1);  // set by the MMA thread when operator tiles did not land
+    volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+    volatile int* s_issued = abort_flag + 1;    // operator chunks whose copy was issued (warp 0)
+    volatile int* s_consumed = abort_flag + 2;  // operator chunks seen landed (warp 1)
 
     const int r = blockIdx.x, mt = blockIdx.y, b0 = blockIdx.z * BP;
     const int MT = N / CX_M, NC = N / CX_KC;
@@ -434,182 +470,222 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
                      "r"(NCOLS));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
-    if (threadIdx.x == 0) {
-        for (int q = 0; q < 2 * CX_S + 1; ++q)
-            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&full[q])));
+    if (threadIdx.x == 32) {
+        for (int q = 0; q < CX_S; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&a_full[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(&x_full[q])), "r"(XW));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&stage_free[q])));
+        }
+        for (int q = 0; q < 2; ++q) {
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(&acc_full[q])));
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 128;" ::"r"(smem_addr(&acc_free[q])));
+        }
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(drain)));
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        *s_fail = 0;
+        *abort_flag = 0;
+        *s_issued = 0;
+        *s_consumed = 0;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     const uint32_t tmem = *tmem_slot;
 
-    // instruction descriptor: D f32, A and B tf32, both K-major, N = BP, M = 128
-    const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BP >> 3) << 17) | ((uint32_t)(CX_M >> 4) << 24);
-    const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-    const int col0 = (warp >> 2) * HB;
-    float zr[HB], zi[HB];
+    // every role runs its loop on whole warps (lane 0 issues; waits are polled by lane 0 and broadcast), so the warps
+    // stay converged for the CTA barrier at the end
+    if (warp == 0) {  // operator tiles, chunk after chunk, as soon as a stage is free
+        for (int kc = 0; kc < NC; ++kc) {
+            const int s = kc % CX_S, u = kc / CX_S;
+            if (u > 0 && !warp_wait(smem_addr(&stage_free[s]), (uint32_t)((u - 1) & 1), abort_flag)) {
+                if (lane == 0) *abort_flag = 1;
+                break;
+            }
+            if (lane == 0) {
+                mbar_expect_bulk(smem_addr(&a_full[s]), smem_addr(smem_raw + s * STAGE), Wr + (size_t)kc * 4 * CX_TILE,
+                                 A_BYTES);
+                *s_issued = kc + 1;
+            }
+            __syncwarp();
+        }
+    } else if (warp == 1) {
+        {  // the MMAs of chunk after chunk
+            const uint32_t idesc = (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(BP >> 3) << 17) |
+                                   ((uint32_t)(CX_M >> 4) << 24);
+            constexpr uint32_t SBO = (CX_KC / 4) * 128;
+            for (int kc = 0; kc < NC; ++kc) {
+                // accumulator set of chunk kc: kc % 2 (its v-th use, v = kc / 2); every chunk is folded into FP32
+                // registers on its own (accumulating two chunks in tensor memory measured a larger error)
+                const int s = kc % CX_S, u = kc / CX_S, be = kc & 1, v = kc >> 1;
+                if (!warp_wait(smem_addr(&a_full[s]), (uint32_t)(u & 1), abort_flag)) {
+                    if (lane == 0) *abort_flag = 1;
+                    break;
+                }
+                if (lane == 0) *s_consumed = kc + 1;
+                if (!warp_wait(smem_addr(&x_full[s]), (uint32_t)(u & 1), abort_flag) ||
+                    (v > 0 && !warp_wait(smem_addr(&acc_free[be]), (uint32_t)((v - 1) & 1), abort_flag))) {
+                    if (lane == 0) *abort_flag = 1;
+                    break;
+                }
+                asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+                if (lane == 0) {
+                    const uint32_t d = tmem + (uint32_t)(be * NACC);
+                    const uint32_t a0 = smem_addr(smem_raw + s * STAGE), x0 = a0 + A_BYTES;
 #pragma unroll
-    for (int q = 0; q < HB; ++q) zr[q] = zi[q] = 0.f;
-    bool ok = true;
-    int issued = 0, consumed = 0;  // operator chunks whose bulk copy was issued / seen landed (thread 0)
-
-    // fold accumulator set s (one chunk's partial sums) into zr, zi
-    auto promote = [&](int s) {
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t base = tmem + lane_base + (uint32_t)(s * NACC + col0);
-#pragma unroll
-        for (int c = 0; c < HB; c += 8) {
-            uint32_t p1[8], p2[8], p3[8];
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(p1[0]), "=r"(p1[1]), "=r"(p1[2]), "=r"(p1[3]), "=r"(p1[4]), "=r"(p1[5]), "=r"(p1[6]),
-                           "=r"(p1[7])
-                         : "r"(base + c));
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(p2[0]), "=r"(p2[1]), "=r"(p2[2]), "=r"(p2[3]), "=r"(p2[4]), "=r"(p2[5]), "=r"(p2[6]),
-                           "=r"(p2[7])
-                         : "r"(base + BP + c));
-            asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
-                         : "=r"(p3[0]), "=r"(p3[1]), "=r"(p3[2]), "=r"(p3[3]), "=r"(p3[4]), "=r"(p3[5]), "=r"(p3[6]),
-                           "=r"(p3[7])
-                         : "r"(base + 2 * BP + c));
-            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                zr[c + q] += __uint_as_float(p1[q]) - __uint_as_float(p2[q]);
-                zi[c + q] += __uint_as_float(p3[q]);
+                    for (int k8 = 0; k8 < CX_KC / 8; ++k8) {
+                        const uint32_t ko = k8 * 256;
+                        const uint64_t reh = desc_kmajor(a0 + ko, 128, SBO), rel = desc_kmajor(a0 + CX_TILE * 4 + ko, 128, SBO);
+                        const uint64_t imh = desc_kmajor(a0 + 2 * CX_TILE * 4 + ko, 128, SBO);
+                        const uint64_t iml = desc_kmajor(a0 + 3 * CX_TILE * 4 + ko, 128, SBO);
+                        const uint64_t xrh = desc_kmajor(x0 + ko, 128, SBO), xrl = desc_kmajor(x0 + XT * 4 + ko, 128, SBO);
+                        const uint64_t xih = desc_kmajor(x0 + 2 * XT * 4 + ko, 128, SBO);
+                        const uint64_t xil = desc_kmajor(x0 + 3 * XT * 4 + ko, 128, SBO);
+                        const uint64_t xnh = desc_kmajor(x0 + 4 * XT * 4 + ko, 128, SBO);
+                        const uint64_t xnl = desc_kmajor(x0 + 5 * XT * 4 + ko, 128, SBO);
+                        const uint32_t acc = k8 == 0 ? 0u : 1u;
+                        mma_tf32(d, reh, xrh, idesc, acc);  // Re z = Re W Re y + Im W (-Im y)
+                        mma_tf32(d, reh, xrl, idesc, 1u);
+                        mma_tf32(d, rel, xrh, idesc, 1u);
+                        mma_tf32(d, imh, xnh, idesc, 1u);
+                        mma_tf32(d, imh, xnl, idesc, 1u);
+                        mma_tf32(d, iml, xnh, idesc, 1u);
+                        mma_tf32(d + BP, imh, xrh, idesc, acc);  // Im z = Im W Re y + Re W Im y
+                        mma_tf32(d + BP, imh, xrl, idesc, 1u);
+                        mma_tf32(d + BP, iml, xrh, idesc, 1u);
+                        mma_tf32(d + BP, reh, xih, idesc, 1u);
+                        mma_tf32(d + BP, reh, xil, idesc, 1u);
+                        mma_tf32(d + BP, rel, xih, idesc, 1u);
+                    }
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_addr(&stage_free[s]))
+                                 : "memory");
+                    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                                     smem_addr(&acc_full[be]))
+                                 : "memory");
+                }
+                __syncwarp();
             }
         }
-    };
-    auto issue_a = [&](int kc) {  // thread 0: the operator tiles of chunk kc into stage kc % CX_S
-        const int s = kc % CX_S;
-        mbar_expect_bulk(smem_addr(&full[s]), smem_addr(smem_raw + s * STAGE), Wr + (size_t)kc * 4 * CX_TILE, A_BYTES);
-    };
-
-    // image rows: thread t loads 4 consecutive complex values (t % 4: which quad of the chunk) of image t / 4
-    constexpr int XTHREADS = BP * (CX_KC / 4);
-    const int xb = threadIdx.x / (CX_KC / 4), xq = threadIdx.x % (CX_KC / 4);
-    const bool xon = threadIdx.x < XTHREADS;
-    const bool xlive = xon && b0 + xb < nimg;
-    const float4* ysrc = reinterpret_cast<const float4*>(Y + (long long)(b0 + xb) * img_stride + yrow + 4 * xq);
-    float4 ya = make_float4(0.f, 0.f, 0.f, 0.f), yb = ya;
-    auto load_x = [&](int kc) {
-        if (xlive) {
-            ya = ysrc[kc * (CX_KC / 2)];
-            yb = ysrc[kc * (CX_KC / 2) + 1];
-        }
-    };
-    if (threadIdx.x == 0) {
-        for (int kc = 0; kc < 2 && kc < NC; ++kc) issue_a(kc);
-        issued = NC < 2 ? NC : 2;
-    }
-    load_x(0);
-
-    for (int kc = 0; kc < NC; ++kc) {
-        const int s = kc % CX_S;
-        unsigned char* st = smem_raw + s * STAGE;
-        if (kc >= 2) {
-            // chunk kc-2: its MMAs read stage (kc+2) % CX_S and wrote accumulator set kc % 2
-            const int w = mbar_wait(smem_addr(&done[(kc - 2) % CX_S]), (uint32_t)(((kc - 2) / CX_S) & 1)) ? 1 : 0;
-            ok = __syncthreads_and(w && !*s_fail) != 0;
-            if (!ok) break;
-            promote(kc & 1);
-        }
-        if (threadIdx.x == 0 && kc + 2 < NC) {
-            issue_a(kc + 2);
-            issued = kc + 3;
-        }
-        if (xon) {  // the image tiles of chunk kc: Re hi, Re lo, Im hi, Im lo
-            const float re[4] = {ya.x, ya.z, yb.x, yb.z}, im[4] = {ya.y, ya.w, yb.y, yb.w};
-            uint32_t rh[4], rl[4], ih[4], il[4];
+    } else if (warp < 4) {  // image tiles: item e = (image e / 4, quad e % 4 of the chunk's 16 columns)
+        const int t = threadIdx.x - 64;
+        constexpr int ITEMS = BP * (CX_KC / 4);
+        constexpr int PER = (ITEMS + XW - 1) / XW;
+        // three chunks of image values in flight: the loads of chunk kc + 3 are issued once chunk kc is stored
+        float4 ya0[PER], yb0[PER], ya1[PER], yb1[PER], ya2[PER], yb2[PER];
+        auto load = [&](int kc, float4 (&ya)[PER], float4 (&yb)[PER]) {
 #pragma unroll
-            for (int q = 0; q < 4; ++q) {
-                rh[q] = to_tf32(re[q]);
-                rl[q] = to_tf32(re[q] - __uint_as_float(rh[q]));
-                ih[q] = to_tf32(im[q]);
-                il[q] = to_tf32(im[q] - __uint_as_float(ih[q]));
-            }
-            const int off = ((xb / 8) * (CX_KC / 4) + xq) * 128 + (xb % 8) * 16;
-            unsigned char* xt = st + A_BYTES;
-            *reinterpret_cast<uint4*>(xt + off) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
-            *reinterpret_cast<uint4*>(xt + XT * 4 + off) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
-            *reinterpret_cast<uint4*>(xt + 2 * XT * 4 + off) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
-            *reinterpret_cast<uint4*>(xt + 3 * XT * 4 + off) = make_uint4(il[0], il[1], il[2], il[3]);
-        }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-        __syncthreads();
-        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        if (threadIdx.x == 0) {
-            const bool landed = !*s_fail && mbar_wait(smem_addr(&full[s]), (uint32_t)((kc / CX_S) & 1));
-            if (landed) {
-                consumed = kc + 1;
-                const uint32_t d = tmem + (uint32_t)((kc & 1) * NACC);
-                const uint32_t a0 = smem_addr(st), x0 = smem_addr(st + A_BYTES);
-                constexpr uint32_t SBO = (CX_KC / 4) * 128;
-#pragma unroll
-                for (int k8 = 0; k8 < CX_KC / 8; ++k8) {
-                    const uint32_t ko = k8 * 256;
-                    const uint64_t reh = desc_kmajor(a0 + ko, 128, SBO), rel = desc_kmajor(a0 + CX_TILE * 4 + ko, 128, SBO);
-                    const uint64_t imh = desc_kmajor(a0 + 2 * CX_TILE * 4 + ko, 128, SBO);
-                    const uint64_t iml = desc_kmajor(a0 + 3 * CX_TILE * 4 + ko, 128, SBO);
-                    const uint64_t xrh = desc_kmajor(x0 + ko, 128, SBO), xrl = desc_kmajor(x0 + XT * 4 + ko, 128, SBO);
-                    const uint64_t xih = desc_kmajor(x0 + 2 * XT * 4 + ko, 128, SBO);
-                    const uint64_t xil = desc_kmajor(x0 + 3 * XT * 4 + ko, 128, SBO);
-                    const uint32_t fresh = k8 > 0 ? 1u : 0u;
-                    mma_tf32(d, reh, xrh, idesc, fresh);  // P1 = Re W Re y
-                    mma_tf32(d, reh, xrl, idesc, 1u);
-                    mma_tf32(d, rel, xrh, idesc, 1u);
-                    mma_tf32(d + BP, imh, xih, idesc, fresh);  // P2 = Im W Im y
-                    mma_tf32(d + BP, imh, xil, idesc, 1u);
-                    mma_tf32(d + BP, iml, xih, idesc, 1u);
-                    mma_tf32(d + 2 * BP, imh, xrh, idesc, fresh);  // P3 = Im W Re y + Re W Im y
-                    mma_tf32(d + 2 * BP, imh, xrl, idesc, 1u);
-                    mma_tf32(d + 2 * BP, iml, xrh, idesc, 1u);
-                    mma_tf32(d + 2 * BP, reh, xih, idesc, 1u);
-                    mma_tf32(d + 2 * BP, reh, xil, idesc, 1u);
-                    mma_tf32(d + 2 * BP, rel, xih, idesc, 1u);
+            for (int j = 0; j < PER; ++j) {
+                const int e = t + j * XW, xb = e / (CX_KC / 4), xq = e % (CX_KC / 4);
+                ya[j] = yb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (kc < NC && e < ITEMS && b0 + xb < nimg) {
+                    const float4* src = reinterpret_cast<const float4*>(Y + (long long)(b0 + xb) * img_stride + yrow +
+                                                                        kc * CX_KC + 4 * xq);
+                    ya[j] = src[0];
+                    yb[j] = src[1];
                 }
             }
-            // commit even when the tiles did not land (no MMA issued then), so the done barriers keep their phases;
-            // the flag stops every thread at its next check
-            asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
-                             smem_addr(&done[s]))
-                         : "memory");
-            if (!landed) *s_fail = 1;
+        };
+        // store chunk kc (values in ya, yb) into its stage, then load chunk kc + 3 into the same registers
+        auto step = [&](int kc, float4 (&ya)[PER], float4 (&yb)[PER]) -> bool {
+            const int s = kc % CX_S, u = kc / CX_S;
+            if (u > 0 && !warp_wait(smem_addr(&stage_free[s]), (uint32_t)((u - 1) & 1), abort_flag)) {
+                if (lane == 0) *abort_flag = 1;
+                return false;
+            }
+            unsigned char* xt = smem_raw + s * STAGE + A_BYTES;
+#pragma unroll
+            for (int j = 0; j < PER; ++j) {
+                const int e = t + j * XW, xb = e / (CX_KC / 4), xq = e % (CX_KC / 4);
+                if (e >= ITEMS) continue;
+                const float re[4] = {ya[j].x, ya[j].z, yb[j].x, yb[j].z}, im[4] = {ya[j].y, ya[j].w, yb[j].y, yb[j].w};
+                uint32_t rh[4], rl[4], ih[4], il[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    rh[q] = to_tf32(re[q]);
+                    rl[q] = to_tf32(re[q] - __uint_as_float(rh[q]));
+                    ih[q] = to_tf32(im[q]);
+                    il[q] = to_tf32(im[q] - __uint_as_float(ih[q]));
+                }
+                const int off = ((xb / 8) * (CX_KC / 4) + xq) * 128 + (xb % 8) * 16;
+                *reinterpret_cast<uint4*>(xt + off) = make_uint4(rh[0], rh[1], rh[2], rh[3]);
+                *reinterpret_cast<uint4*>(xt + XT * 4 + off) = make_uint4(rl[0], rl[1], rl[2], rl[3]);
+                *reinterpret_cast<uint4*>(xt + 2 * XT * 4 + off) = make_uint4(ih[0], ih[1], ih[2], ih[3]);
+                *reinterpret_cast<uint4*>(xt + 3 * XT * 4 + off) = make_uint4(il[0], il[1], il[2], il[3]);
+                constexpr uint32_t SG = 0x80000000u;  // -Im y: the sign flipped, exactly
+                *reinterpret_cast<uint4*>(xt + 4 * XT * 4 + off) = make_uint4(ih[0] ^ SG, ih[1] ^ SG, ih[2] ^ SG, ih[3] ^ SG);
+                *reinterpret_cast<uint4*>(xt + 5 * XT * 4 + off) = make_uint4(il[0] ^ SG, il[1] ^ SG, il[2] ^ SG, il[3] ^ SG);
+            }
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            mbar_arrive(smem_addr(&x_full[s]));
+            load(kc + 3, ya, yb);
+            return true;
+        };
+        load(0, ya0, yb0);
+        load(1, ya1, yb1);
+        load(2, ya2, yb2);
+        for (int kc = 0; kc < NC; kc += 3) {
+            if (!step(kc, ya0, yb0)) break;
+            if (kc + 1 < NC && !step(kc + 1, ya1, yb1)) break;
+            if (kc + 2 < NC && !step(kc + 2, ya2, yb2)) break;
         }
-        if (kc + 1 < NC) load_x(kc + 1);
-    }
-    if (ok) {  // the last two chunks
-        for (int kc = NC - 2 > 0 ? NC - 2 : 0; kc < NC; ++kc) {
-            const int w = mbar_wait(smem_addr(&done[kc % CX_S]), (uint32_t)((kc / CX_S) & 1)) ? 1 : 0;
-            ok = __syncthreads_and(w && !*s_fail) != 0;
-            if (!ok) break;
-            promote(kc & 1);
+    } else {  // warps 4-7: fold every accumulator set (TMEM lanes 32 (warp % 4) ..) into FP32 registers
+        const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
+        float zr[BP], zi[BP];
+#pragma unroll
+        for (int q = 0; q < BP; ++q) zr[q] = zi[q] = 0.f;
+        bool ok = true;
+        // all of one accumulator's columns are loaded before the single wait for them
+        auto fold = [&](uint32_t addr, float (&z)[BP]) {
+            uint32_t t[BP];
+#pragma unroll
+            for (int c = 0; c < BP; c += 16)
+                asm volatile(
+                    "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, "
+                    "[%16];"
+                    : "=r"(t[c]), "=r"(t[c + 1]), "=r"(t[c + 2]), "=r"(t[c + 3]), "=r"(t[c + 4]), "=r"(t[c + 5]),
+                      "=r"(t[c + 6]), "=r"(t[c + 7]), "=r"(t[c + 8]), "=r"(t[c + 9]), "=r"(t[c + 10]), "=r"(t[c + 11]),
+                      "=r"(t[c + 12]), "=r"(t[c + 13]), "=r"(t[c + 14]), "=r"(t[c + 15])
+                    : "r"(addr + c));
+            asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+            for (int q = 0; q < BP; ++q) z[q] += __uint_as_float(t[q]);
+        };
+        for (int kc = 0; kc < NC; ++kc) {
+            const int be = kc & 1, v = kc >> 1;
+            if (!warp_wait(smem_addr(&acc_full[be]), (uint32_t)(v & 1), abort_flag)) {
+                if (lane == 0) *abort_flag = 1;
+                ok = false;
+                break;
+            }
+            asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+            const uint32_t base = tmem + lane_base + (uint32_t)(be * NACC);
+            fold(base, zr);
+            fold(base + BP, zi);
+            asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+            mbar_arrive(smem_addr(&acc_free[be]));
+        }
+        if (ok) {
+            const int o = mt * CX_M + (warp & 3) * 32 + lane;
+#pragma unroll
+            for (int q = 0; q < BP; ++q) {
+                const int b = b0 + q;
+                if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = make_float2(zr[q], zi[q]);
+            }
         }
     }
-    if (!ok && threadIdx.x == 0) {
-        // a wait gave up: before the tensor memory is freed and the CTA leaves, every MMA it issued (one more commit
-        // to the spare barrier) and every operator copy it issued (the stages' byte counts) must have completed;
-        // both waits are bounded. Flag 1: this launch's dense rows were not written; 2: even the drain ran out.
+    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+    __syncthreads();
+    if (*abort_flag && threadIdx.x == 32) {
+        // a wait gave up: before the tensor memory is freed and the CTA leaves, every MMA issued (one more commit to
+        // the spare barrier) and every operator copy issued (the stages' byte counts) must have completed; the waits
+        // are bounded. Flag 1: this launch's dense rows were not written; 2: even the drain ran out.
         asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
                          smem_addr(drain))
                      : "memory");
         bool drained = mbar_wait(smem_addr(drain), 0u);
-        for (int kc = consumed; kc < issued; ++kc)  // at most three outstanding copies, in distinct stages
-            drained = mbar_wait(smem_addr(&full[kc % CX_S]), (uint32_t)((kc / CX_S) & 1)) && drained;
+        for (int kc = *s_consumed; kc < *s_issued; ++kc)  // at most CX_S outstanding copies, in distinct stages
+            drained = mbar_wait(smem_addr(&a_full[kc % CX_S]), (uint32_t)((kc / CX_S) & 1)) && drained;
         atomicMax(err, drained ? 1 : 2);
     }
-    if (ok) {
-        const int o = mt * CX_M + (warp & 3) * 32 + lane;
-#pragma unroll
-        for (int q = 0; q < HB; ++q) {
-            const int b = b0 + col0 + q;
-            if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = make_float2(zr[q], zi[q]);
-        }
-    }
-    asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
 }
@@ -618,7 +694,7 @@ template <int BP>
 static int launch_cx(int n, int nimg, int nrows, const int* rows, const void* Ws, const void* Y, long long img_stride,
                      void* Zd, int* err, cudaStream_t st) {
     const int N = 1 << n;
-    const size_t smem = (size_t)CX_S * (4 * CX_TILE * 4 + 4 * BP * CX_KC * 4) + 128;  // stages, barriers, slots
+    const size_t smem = (size_t)CX_S * (4 * CX_TILE * 4 + 6 * BP * CX_KC * 4) + CX_BAR_BYTES;  // stages, barriers
     auto kern = dense_cx_kernel<BP>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
     dim3 grid(nrows, N / CX_M, (nimg + BP - 1) / BP);
