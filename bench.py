@@ -229,12 +229,14 @@ def measured_hbm_peak():
 
 def hbm_rooflines(ktimer, pipe):
     """Achieved HBM GB/s of the offset-FFT kernels in the timed region (CUDA events on their stream) against the
-    measured copy bandwidth; algorithmic bytes per launch: the image (FP64) read and the packed rows (complex64)
-    written by the image pack, the packed rows read and the three FP32 partial images written by the unpack."""
+    measured copy bandwidth; algorithmic bytes per launch: the image read (the FP32 hi plane of a float-float outer
+    state, else the FP64 image) and the packed rows (complex64) written by the image pack, the packed rows read and
+    the three FP32 partial images written by the unpack."""
     N, B = pipe.plan.N, pipe.B
     isz = pipe.real.itemsize
     y_bytes = B * (4 * N) * N * 2 * isz  # packed rows: 2L = 4N rows of N complex per image
-    bytes_ = {"pack_fft_kernel (image)": B * N * N * 8 + y_bytes,
+    img_bytes = 4 if getattr(pipe, "ff_state", False) else 8
+    bytes_ = {"pack_fft_kernel (image)": B * N * N * img_bytes + y_bytes,
               "ifft_unpack_kernel": y_bytes + 3 * B * N * N * isz}
     names = {"pack_image": "pack_fft_kernel (image)", "unpack": "ifft_unpack_kernel"}
     peak, src = measured_hbm_peak()
