@@ -70,7 +70,29 @@ struct OuterStepArgs {
     double g1_a0;
     double g1_om_a[OS_MAX_STEPS];
     double g1_om_1[OS_MAX_STEPS];
+    // the same coefficients rounded to FP32 once on the host (the register-resident kernel runs no FP64 per thread):
+    // the stencil's, and hi + lo splits of the outer ones
+    float g1f_a0;
+    float g1f_a[OS_MAX_STEPS];
+    float g1f_1[OS_MAX_STEPS];
+    float oa_hi, oa_lo, o1_hi, o1_lo, a0_hi, a0_lo;
 };
+
+// fill the FP32 copies of the coefficients (host)
+static void fill_f32_coefficients(OuterStepArgs& A) {
+    auto split = [](double v, float& hi, float& lo) {
+        hi = (float)v;
+        lo = (float)(v - (double)hi);
+    };
+    A.g1f_a0 = (float)A.g1_a0;
+    for (int k = 0; k + 1 < A.g1_deg && k < OS_MAX_STEPS; ++k) {
+        A.g1f_a[k] = (float)A.g1_om_a[k];
+        A.g1f_1[k] = (float)A.g1_om_1[k];
+    }
+    split(A.om_a, A.oa_hi, A.oa_lo);
+    split(A.om_1, A.o1_hi, A.o1_lo);
+    split(A.a0, A.a0_hi, A.a0_lo);
+}
 
 template <typename TS, typename TP, int n, int BAND>
 __global__ void __launch_bounds__(OS_THREADS) outer_step_kernel(const OuterStepArgs A) {
@@ -377,7 +399,7 @@ __global__ void __launch_bounds__(32 * (BAND / (1024 >> n)), (1 << n) <= 256 ? 2
                 p[R - 1][2 * q + 1] = fmaf(-om_a, tb.x, p[R - 1][2 * q + 1]);
             }
         };
-        const float a0 = (float)A.g1_a0;
+        const float a0 = A.g1f_a0;
 #pragma unroll
         for (int r = 0; r < R; ++r)
 #pragma unroll
@@ -388,13 +410,13 @@ __global__ void __launch_bounds__(32 * (BAND / (1024 >> n)), (1 << n) <= 256 ? 2
         publish(cA, 0);
         int k = 1;
         for (; k + 1 < A.g1_deg; k += 2) {
-            step(cA, cB, (float)A.g1_om_a[k - 1], (float)A.g1_om_1[k - 1], (k - 1) & 1);
+            step(cA, cB, A.g1f_a[k - 1], A.g1f_1[k - 1], (k - 1) & 1);
             publish(cB, k & 1);
-            step(cB, cA, (float)A.g1_om_a[k], (float)A.g1_om_1[k], k & 1);
+            step(cB, cA, A.g1f_a[k], A.g1f_1[k], k & 1);
             publish(cA, (k + 1) & 1);
         }
         if (k < A.g1_deg) {
-            step(cA, cB, (float)A.g1_om_a[k - 1], (float)A.g1_om_1[k - 1], (k - 1) & 1);
+            step(cA, cB, A.g1f_a[k - 1], A.g1f_1[k - 1], (k - 1) & 1);
             publish(cB, k & 1);
             in_b = true;
         }
@@ -424,12 +446,16 @@ __global__ void __launch_bounds__(32 * (BAND / (1024 >> n)), (1 << n) <= 256 ? 2
     // om_a r + om_1 (x - x_prev) in FP32 with the coefficients carried as hi + lo, added to x with an exact
     // two-sum, so the state keeps about 48 bits while no FP64 instruction runs (the FP64 pipe of this GPU is a small
     // fraction of its FP32 pipe)
-    const double oa = A.om_img ? A.om_img[2 * img] : A.om_a;
-    const double o1 = A.om_img ? A.om_img[2 * img + 1] : A.om_1;
     if constexpr (FF) {
-        const float oah = (float)oa, oal = (float)(oa - (double)oah);
-        const float o1h = (float)o1, o1l = (float)(o1 - (double)o1h);
-        const float a0h = (float)A.a0, a0l = (float)(A.a0 - (double)a0h);
+        float oah = A.oa_hi, oal = A.oa_lo, o1h = A.o1_hi, o1l = A.o1_lo;
+        if (A.om_img) {  // per-image coefficients (slot-level serving): split here
+            const double oa = A.om_img[2 * img], o1 = A.om_img[2 * img + 1];
+            oah = (float)oa;
+            oal = (float)(oa - (double)oah);
+            o1h = (float)o1;
+            o1l = (float)(o1 - (double)o1h);
+        }
+        const float a0h = A.a0_hi, a0l = A.a0_lo;
         const size_t fo = gbase + (size_t)img * N * N;  // hi plane of this thread's first row; lo plane N^2 further
 #pragma unroll
         for (int r = 0; r < R; ++r) {
@@ -471,6 +497,8 @@ __global__ void __launch_bounds__(32 * (BAND / (1024 >> n)), (1 << n) <= 256 ? 2
         }
         return;
     }
+    const double oa = A.om_img ? A.om_img[2 * img] : A.om_a;
+    const double o1 = A.om_img ? A.om_img[2 * img + 1] : A.om_1;
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         const size_t gi = gbase + (size_t)r * N;
@@ -635,6 +663,7 @@ int outer_step(int dtype, int parts_dtype, int n, int nimg, const double* y, con
             A.g1_om_1[k - 1] = g1_coef[2 * k];
         }
     }
+    fill_f32_coefficients(A);
     // FP32 stencil on FP32 partial images: the register-resident form where it exists, unless the shared-memory
     // form is asked for
     if (!shared_form && dtype == ADRT_F32 && parts_dtype == ADRT_F32 && n >= 6 && n <= 9)
@@ -675,6 +704,7 @@ int outer_step_ff(int n, int nimg, const float* y, const float* p0, const float*
             A.g1_om_1[k - 1] = g1_coef[2 * k];
         }
     }
+    fill_f32_coefficients(A);
     return dispatch_os_reg<true>(n, A, nimg, band, st);
 }
 
