@@ -9,7 +9,9 @@ three real image-space partial sums (3, B, N, N); outer state x, x_prev, y (B, N
 precision in fp64 mode, where everything is FP64).
 """
 
+import contextlib
 import ctypes
+import gc
 import weakref
 
 import numpy as np
@@ -40,6 +42,22 @@ def fuse_ops(ops):
 
 def _cdtype(real):
     return torch.complex64 if real == torch.float32 else torch.complex128
+
+
+@contextlib.contextmanager
+def graph_capture(graph, stream):
+    """torch.cuda.graph with Python's cyclic garbage collector paused for the capture: a collection inside it could
+    destroy CUDA objects (graphs, events, streams) of unreachable pipelines, which invalidates a global-mode
+    capture ("operation failed due to a previous error during capture")."""
+    enabled = gc.isenabled()
+    gc.collect()
+    gc.disable()
+    try:
+        with torch.cuda.graph(graph, stream=stream):
+            yield
+    finally:
+        if enabled:
+            gc.enable()
 
 
 class RowTables:
@@ -609,14 +627,14 @@ class Pipeline:
             side.synchronize()
             self.graph = torch.cuda.CUDAGraph()
             before = self.tables.count
-            with torch.cuda.graph(self.graph, stream=side):
+            with graph_capture(self.graph, side):
                 self.x_out = self.apply(self.b_in)
             self.graph_count = self.tables.count - before  # level-rows of one replay
             # a second graph on a second input buffer: host batches alternate between the two, so that the copy of
             # the next batch (on its own stream) overlaps the graph of the current one
             self.b_in2 = torch.zeros_like(self.b_in)
             self.graph2 = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph2, stream=side):
+            with graph_capture(self.graph2, side):
                 x2 = self.apply(self.b_in2)
             self.tables.count -= self.graph_count
             assert x2.data_ptr() == self.x_out.data_ptr()

@@ -26,6 +26,7 @@ import numpy as np
 import torch
 
 from . import _lib as C
+from .device import graph_capture
 
 
 def _nblk(nimg, length, sms):
@@ -84,7 +85,7 @@ class _Solver:
                 side.wait_stream(torch.cuda.current_stream(self.device))
                 with torch.cuda.stream(side):
                     g = torch.cuda.CUDAGraph()
-                    with torch.cuda.graph(g, stream=side):
+                    with graph_capture(g, side):
                         step_block()
                 torch.cuda.current_stream(self.device).wait_stream(side)
                 self.graph = g

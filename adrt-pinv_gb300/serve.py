@@ -29,7 +29,7 @@ from collections import deque
 import numpy as np
 import torch
 
-from .device import Pipeline
+from .device import Pipeline, graph_capture
 from .plan import outer_coeffs
 
 
@@ -168,7 +168,7 @@ class SlotLane:
         for b in self.sizes:
             for ph in range(3):
                 g = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(g, stream=self.stream):
+                with graph_capture(g, self.stream):
                     self._step_eager(ph, b)
                 self.graphs[(b, ph)] = g
         self.s = 0  # global step counter (the buffer rotation phase is s % 3)

@@ -16,7 +16,7 @@ class UnevenBatch:
         """groups: [(inverse, count)], one entry per class; an inverse may appear more than once (a large class split
         into several concurrent parts), each entry getting its own pipeline. With a tuner (tune.Tuner) and the
         classes' sinograms, every class's launch configuration is autotuned on its own data before the capture."""
-        from .device import Pipeline
+        from .device import Pipeline, graph_capture
 
         self.groups = [(inv, int(c)) for inv, c in groups if int(c) > 0]
         self.device = torch.device(device)
@@ -36,7 +36,7 @@ class UnevenBatch:
             cap.synchronize()
             self.graph = torch.cuda.CUDAGraph()
             self.outputs = []
-            with torch.cuda.graph(self.graph, stream=cap):
+            with graph_capture(self.graph, cap):
                 for st, pipe, x in zip(self.streams, self.pipes, self.inputs):
                     st.wait_stream(cap)
                     with torch.cuda.stream(st):
@@ -84,7 +84,7 @@ class PersistentUnevenBatch:
         import numpy as np
 
         from . import _lib as C
-        from .device import Pipeline
+        from .device import Pipeline, graph_capture
         from .plan import outer_coeffs
 
         self.groups = [(inv, int(c)) for inv, c in groups if int(c) > 0]
@@ -138,7 +138,7 @@ class PersistentUnevenBatch:
             self._run(cap)  # and one eager run of the lock-step schedule
             cap.synchronize()
             self.graph = torch.cuda.CUDAGraph()
-            with torch.cuda.graph(self.graph, stream=cap):
+            with graph_capture(self.graph, cap):
                 self.outputs = self._run(cap)
         torch.cuda.current_stream(self.device).wait_stream(cap)
         self.launches_per_step = None
