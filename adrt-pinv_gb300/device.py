@@ -5,9 +5,9 @@ For a plan, a batch size B and a precision, `Pipeline` owns every device buffer 
   precond                    : the hybrid's P = g1_inv / lorr_inv (fasthybrid.py:108-130)
   apply                      : backproject + fixed-degree outer Chebyshev (fastops.py:247-258, 283-288, 333-338)
 Layouts in HBM (per batch): Y (B, 2L, N) complex rows (pair (0,1) then (2,3), each L offset-frequency rows);
-three real image-space partial sums (3, B, N, N); outer state x, x_prev, y (B, N, N) in FP64 (or the compute
-precision in fp64 mode, where everything is FP64).
-"""
+three real image-space partial sums (3, B, N, N); outer state x, x_prev, x_new as float-float planes (B, 2, N, N)
+FP32 with y FP32 where the register-resident fused outer step runs (FP32 rows and stencil, 64 <= N <= 512), else
+(B, N, N) FP64; the FP64 result (B, N, N) converted once per apply."""
 
 import contextlib
 import ctypes

@@ -3,7 +3,8 @@
 Workload (one step): the hybrid explicit inverse (fastops.FastHybrid.apply semantics) of a batch of 64 noisy
 sinograms of seeded 10-ellipse phantoms at N = 256 (n = 8), inner degrees capped at p = 32, dense low-frequency
 table for d_k > 16, FP32 row engine / FFTs and cross-quadrant preconditioner (--stencil ff|fp64 for the FP64-class
-forms) with FP64 tables and FP64 outer iteration. Metric: whole-job reconstructions per second. Every step's inputs
+forms) with FP64 tables; the outer iteration's state is float-float (FP32 hi/lo planes, about 48 bits) with the FP32
+stencil and FP64 with the others. Metric: whole-job reconstructions per second. Every step's inputs
 (268 MB of FP64 sinograms) exceed the 129 MB L2, so no flush is needed between steps.
 
   value : device-resident sinograms, K timed replays of the captured apply (CUDA events, barrier + sync both sides);
@@ -75,8 +76,8 @@ def config(args, world):
             "N": N, "global_batch": args.batch * world, "p": P_CAP, "dense_cap": DENSE_CAP, "method": "hybrid",
             "precond": "g1",
             "precision": f"fp32 rows/FFT, cross-quadrant inverse {STENCIL_NAMES[getattr(args, 'stencil', STENCIL)]}, "
-                         "fp64 tables and "
-                         "outer state",
+                         "fp64 tables, outer state "
+                         + ("float-float (fp32 hi/lo planes)" if getattr(args, "stencil", STENCIL) == "fp32" else "fp64"),
             "parallelism": f"replicas x{world}", "l2": "inputs (268 MB/step) larger than L2; no flush"}
 
 
