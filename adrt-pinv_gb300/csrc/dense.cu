@@ -436,11 +436,13 @@ __device__ __forceinline__ void mbar_arrive(uint32_t mbar) {
 // the image tiles, warp 1 (one thread) issues the MMAs, warps 4-7 fold each chunk's accumulator set into FP32
 // registers and write the result. Per stage: a_full (operator bytes landed), x_full (64 image-tile arrivals),
 // stage_free (commit of the chunk's MMAs); per accumulator set: acc_full (commit), acc_free (128 fold arrivals).
+// The CTAs of one row (its N / 128 blocks of output rows) form a thread-block cluster: each reads the whole input row
+// while it runs, so the results are written in place only after a cluster barrier at the end, when every CTA of the
+// row has finished reading (no staging buffer, no scatter).
 template <int BP>
 __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg, const int* __restrict__ rows,
-                                                                 const float* __restrict__ Ws,
-                                                                 const float2* __restrict__ Y, long long img_stride,
-                                                                 float2* __restrict__ Zd, int* __restrict__ err) {
+                                                                 const float* __restrict__ Ws, float2* Y,
+                                                                 long long img_stride, int* __restrict__ err) {
     constexpr int A_BYTES = 4 * CX_TILE * 4;  // 32 KB
     constexpr int XT = BP * CX_KC;            // floats per image tile
     constexpr int STAGE = A_BYTES + 6 * XT * 4;  // image tiles: Re hi, Re lo, Im hi, Im lo, -Im hi, -Im lo
@@ -464,6 +466,8 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
     const float* Wr = Ws + ((size_t)r * MT + mt) * NC * 4 * CX_TILE;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long yrow = (long long)rows[r] * N;
+    float zr[BP], zi[BP];  // the fold warps' results (warps 4-7), written after the cluster barrier
+    bool folded = false;
 
     if (warp == 0) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_addr(tmem_slot)),
@@ -629,7 +633,6 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
         }
     } else {  // warps 4-7: fold every accumulator set (TMEM lanes 32 (warp % 4) ..) into FP32 registers
         const uint32_t lane_base = (uint32_t)((warp & 3) * 32) << 16;
-        float zr[BP], zi[BP];
 #pragma unroll
         for (int q = 0; q < BP; ++q) zr[q] = zi[q] = 0.f;
         bool ok = true;
@@ -663,14 +666,7 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
             asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
             mbar_arrive(smem_addr(&acc_free[be]));
         }
-        if (ok) {
-            const int o = mt * CX_M + (warp & 3) * 32 + lane;
-#pragma unroll
-            for (int q = 0; q < BP; ++q) {
-                const int b = b0 + q;
-                if (b < nimg) Zd[((size_t)r * nimg + b) * N + o] = make_float2(zr[q], zi[q]);
-            }
-        }
+        folded = ok;
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();
@@ -687,20 +683,41 @@ __global__ void __launch_bounds__(CX_THREADS, 1) dense_cx_kernel(int N, int nimg
         atomicMax(err, drained ? 1 : 2);
     }
     __syncthreads();
+    // every CTA of the row has read its inputs: the results go in place (none if any role of this CTA gave up)
+    asm volatile("barrier.cluster.arrive.release.aligned;" ::: "memory");
+    asm volatile("barrier.cluster.wait.acquire.aligned;" ::: "memory");
+    if (folded && !*abort_flag) {
+        const int o = mt * CX_M + (warp & 3) * 32 + lane;
+#pragma unroll
+        for (int q = 0; q < BP; ++q) {
+            const int b = b0 + q;
+            if (b < nimg) Y[(long long)b * img_stride + yrow + o] = make_float2(zr[q], zi[q]);
+        }
+    }
     if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(NCOLS));
 }
 
 template <int BP>
-static int launch_cx(int n, int nimg, int nrows, const int* rows, const void* Ws, const void* Y, long long img_stride,
-                     void* Zd, int* err, cudaStream_t st) {
+static int launch_cx(int n, int nimg, int nrows, const int* rows, const void* Ws, void* Y, long long img_stride, int* err,
+                     cudaStream_t st) {
     const int N = 1 << n;
     const size_t smem = (size_t)CX_S * (4 * CX_TILE * 4 + 6 * BP * CX_KC * 4) + CX_BAR_BYTES;  // stages, barriers
     auto kern = dense_cx_kernel<BP>;
     if (int rc = ensure_smem((const void*)kern, smem)) return rc;
-    dim3 grid(nrows, N / CX_M, (nimg + BP - 1) / BP);
-    kern<<<grid, CX_THREADS, smem, st>>>(N, nimg, rows, reinterpret_cast<const float*>(Ws),
-                                         reinterpret_cast<const float2*>(Y), img_stride, reinterpret_cast<float2*>(Zd),
-                                         err);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(nrows, N / CX_M, (nimg + BP - 1) / BP);
+    cfg.blockDim = dim3(CX_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;  // the N / 128 CTAs of a row (at most 8 for N <= 1024)
+    attr[0].val.clusterDim.x = 1;
+    attr[0].val.clusterDim.y = N / CX_M;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kern, N, nimg, rows, reinterpret_cast<const float*>(Ws), reinterpret_cast<float2*>(Y),
+                       img_stride, err);
     return launch_status("dense_cx_kernel");
 }
 
@@ -738,7 +755,7 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
         return ADRT_EINVAL;
     }
     if ((dtype != ADRT_F32 && dtype != ADRT_F64) || n < 1 || n > 11 || nimg < 0 || nrows < 0 ||
-        (nimg && nrows && (!rows || !W || !Y || !Zd))) {
+        (nimg && nrows && (!rows || !W || !Y || (!Zd && use_tc != 3)))) {
         set_error("dense_rows: bad arguments (dtype=%d n=%d nimg=%d nrows=%d)", dtype, n, nimg, nrows);
         return ADRT_EINVAL;
     }
@@ -752,9 +769,9 @@ int dense_rows(int dtype, int n, int nimg, int nrows, const int* rows, const voi
             return ADRT_EINVAL;
         }
         const int bp = tile ? tile : (nimg <= 16 ? 16 : (nimg <= 32 ? 32 : 64));
-        if (bp == 16) rc = launch_cx<16>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
-        else if (bp == 32) rc = launch_cx<32>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
-        else rc = launch_cx<64>(n, nimg, nrows, rows, W, Y, img_stride, Zd, err, st);
+        if (bp == 16) return launch_cx<16>(n, nimg, nrows, rows, W, Y, img_stride, err, st);
+        if (bp == 32) return launch_cx<32>(n, nimg, nrows, rows, W, Y, img_stride, err, st);
+        return launch_cx<64>(n, nimg, nrows, rows, W, Y, img_stride, err, st);  // in place: no Zd, no scatter
     } else if (use_tc == 2) {
         if (dtype != ADRT_F32 || nimg > 16) {
             set_error("dense_rows: the streaming kernel (use_tc = 2) takes FP32 and at most 16 images (nimg=%d)", nimg);

@@ -208,12 +208,13 @@ class RowTables:
         batches; FP64: CUDA cores)."""
         B, R, N = Y.shape
         nd = int(self.rows_dense.numel())
-        if self._zd is None or self._zd.shape[1] != B:
-            self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
         mode = self.dense_mode()
+        if mode != 3 and (self._zd is None or self._zd.shape[1] != B):  # mode 3 writes in place
+            self._zd = torch.empty((nd, B, N), dtype=Y.dtype, device=self.device)
         W = self.split_table(T) if mode == 3 else T
         C.call("adrt_dense_rows", self.code, self.plan.n, B, nd, C.ptr(self.rows_dense), C.ptr(W), C.ptr(Y), R * N,
-               C.ptr(self._zd), C.ptr(self.err), mode, self.dense_tile if mode in (1, 3) else 0, C.stream_handle())
+               None if mode == 3 else C.ptr(self._zd), C.ptr(self.err), mode,
+               self.dense_tile if mode in (1, 3) else 0, C.stream_handle())
 
     def run_ff(self, Y, ops):
         """The op list on the high-condition rows in float-float arithmetic (adrt_rows_ff_run)."""
@@ -608,8 +609,8 @@ class Pipeline:
             total += L * 16 + plan.coef.size * 8
         else:
             total += 2 * nd * N * N * 2 * rs + nd * B * N * 2 * rs
-            if precision == "fp32" and B > 16 and 7 <= plan.n <= 10:  # their pre-split tensor-core form
-                total += 2 * nd * N * N * 16
+            if precision == "fp32" and B > 16 and 7 <= plan.n <= 10:  # their pre-split tensor-core form (in place)
+                total += 2 * nd * N * N * 16 - nd * B * N * 2 * rs
         total += L * 2 * rs + 3 * L * 4 + plan.coef.size * rs  # roots; deg and the row lists; coefficients
         if captured:  # the two input buffers of the captured graphs
             total += 2 * B * 4 * (2 * N - 1) * N * 8

@@ -209,7 +209,7 @@ int adrt_ff_to_f64(int n, int nimg, const float* x, double* out, void* stream);
  * TRANSPOSED (W[r][i][o] = W_r[o][i]) and a CUDA-core kernel streams it once per group of 8 images (small batches,
  * where the product is bound by reading the operators). use_tc = 3 (FP32, 7 <= n <= 10): W is the pre-split table of
  * adrt_dense_split and the tensor cores run the complex-blocked product (operator tiles by bulk copy through a
- * four-stage ring). Otherwise (use_tc = 0) CUDA cores. tile (tensor cores): images per CTA, 16, 32 or 64 (0: chosen
+ * four-stage ring), writing the rows in place (Zd unused, may be NULL). Otherwise (use_tc = 0) CUDA cores. tile (tensor cores): images per CTA, 16, 32 or 64 (0: chosen
  * from nimg). */
 int adrt_dense_rows(int dtype, int n, int nimg, int nrows, const int32_t* rows, const void* W, void* Y,
                     long long img_stride, void* Zd, int32_t* err, int use_tc, int tile, void* stream);
