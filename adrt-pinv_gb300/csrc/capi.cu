@@ -36,6 +36,14 @@ int launch_status(const char* where) {
     return cuda_status(cudaGetLastError(), where);
 }
 
+int launch_ex_status(cudaError_t launched, const char* where) {
+    if (launched != cudaSuccess) {
+        cudaGetLastError();  // the refusal is reported here; leave no stale error for the next launch
+        return cuda_status(launched, where);
+    }
+    return launch_status(where);
+}
+
 int ensure_smem(const void* func, size_t bytes) {
     static std::mutex mu;
     static std::map<const void*, size_t> done;

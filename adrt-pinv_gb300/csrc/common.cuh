@@ -61,6 +61,9 @@ __host__ __device__ constexpr int imin(int a, int b) { return a < b ? a : b; }
 void set_error(const char* fmt, ...);
 int cuda_status(cudaError_t e, const char* where);
 int launch_status(const char* where);
+// the status of a cudaLaunchKernelEx call: its own return value (cluster launches can be refused there), then the
+// launch error state
+int launch_ex_status(cudaError_t launched, const char* where);
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 

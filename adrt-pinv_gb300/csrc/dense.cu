@@ -716,9 +716,9 @@ static int launch_cx(int n, int nimg, int nrows, const int* rows, const void* Ws
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, N, nimg, rows, reinterpret_cast<const float*>(Ws), reinterpret_cast<float2*>(Y),
-                       img_stride, err);
-    return launch_status("dense_cx_kernel");
+    return launch_ex_status(cudaLaunchKernelEx(&cfg, kern, N, nimg, rows, reinterpret_cast<const float*>(Ws),
+                                               reinterpret_cast<float2*>(Y), img_stride, err),
+                            "dense_cx_kernel");
 }
 
 int dense_split(int n, int nrows, const void* W, void* Ws, cudaStream_t st) {

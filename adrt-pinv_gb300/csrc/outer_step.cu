@@ -544,8 +544,7 @@ static int launch_os_reg(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, A);
-    return launch_status("outer_step_reg_kernel");
+    return launch_ex_status(cudaLaunchKernelEx(&cfg, kern, A), "outer_step_reg_kernel");
 }
 
 template <typename TS, typename TP, int n, int BAND>
@@ -572,8 +571,7 @@ static int launch_os_band(const OuterStepArgs& A, int nimg, cudaStream_t st) {
     attr[0].val.clusterDim.z = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kern, A);
-    return launch_status("outer_step_kernel");
+    return launch_ex_status(cudaLaunchKernelEx(&cfg, kern, A), "outer_step_kernel");
 }
 
 // 32-row bands; when the batch's clusters cannot fill the SMs (N <= 256), 16-row bands instead: twice the CTAs per
