@@ -80,6 +80,50 @@ def test_argument_validation_without_gpu(lib):
     assert lib.adrt_cgls_start(None, None, None) == 1 and lib.adrt_pcg_step(None, None) == 1
 
 
+def test_float_float_and_presplit_entries_validate_without_gpu(lib):
+    """The entry points of the float-float outer state, the hi-plane pack and the pre-split dense rows reject bad
+    arguments before any CUDA call (host buffers stand in for device pointers; they are never dereferenced)."""
+    buf = np.zeros(1 << 16)
+    q = buf.ctypes.data_as(ctypes.c_void_p)
+    coef = np.ones(4)
+    cq = coef.ctypes.data_as(ctypes.c_void_p)
+    # pack: an image stride below N^2, not a multiple of 4, or given for sinograms
+    assert lib.adrt_pack_fft(0, 4, 1, 0, 0, q, 8, q, q, 0, None) == 1 and b"src_stride" in lib.adrt_last_error()
+    assert lib.adrt_pack_fft(0, 4, 1, 0, 0, q, 258, q, q, 0, None) == 1
+    assert lib.adrt_pack_fft(0, 4, 1, 1, 1, q, 512, q, q, 0, None) == 1
+    # float-float outer step: only 64 <= N <= 512, bands 16 / 32, a G_1 degree with its coefficients
+    args = lambda n, pc, deg, band: (n, 2, q, q, q, q, q, q, q, 0.5, 0.25, 0.0, pc, deg, cq, None, band, None)
+    assert lib.adrt_outer_step_ff(*args(5, 1, 3, 0)) == 1 and b"6..9" in lib.adrt_last_error()
+    assert lib.adrt_outer_step_ff(*args(10, 1, 3, 0)) == 1
+    assert lib.adrt_outer_step_ff(*args(8, 1, 3, 48)) == 1
+    assert lib.adrt_outer_step_ff(*args(8, 1, 0, 0)) == 1
+    assert lib.adrt_outer_step_ff(*args(8, 3, 3, 0)) == 1
+    assert lib.adrt_ff_to_f64(12, 1, q, q, None) == 1
+    # pre-split dense rows: the split for 7 <= n <= 10 only; use_tc = 3 takes FP32, 7 <= n <= 10 and an error flag
+    assert lib.adrt_dense_split(6, 1, q, q, None) == 1 and lib.adrt_dense_split(11, 1, q, q, None) == 1
+    rows = np.zeros(1, dtype=np.int32)
+    rq = rows.ctypes.data_as(ctypes.c_void_p)
+    assert lib.adrt_dense_rows(1, 8, 4, 1, rq, q, q, 256, None, q, 3, 0, None) == 1  # FP64
+    assert lib.adrt_dense_rows(0, 6, 4, 1, rq, q, q, 64, None, q, 3, 0, None) == 1  # n < 7
+    assert lib.adrt_dense_rows(0, 8, 4, 1, rq, q, q, 256, None, None, 3, 0, None) == 1  # no error flag
+    assert lib.adrt_dense_rows(0, 8, 4, 1, rq, q, q, 256, None, q, 1, 0, None) == 1  # staging needed for use_tc 1
+    assert lib.adrt_dense_rows(0, 8, 4, 1, rq, q, q, 256, None, q, 3, 48, None) == 1  # tile
+
+
+def test_outer_state_format_choice(pkg):
+    """Float-float outer state where the register-resident outer step runs (FP32 rows and stencil, 64 <= N <= 512);
+    FP64 state otherwise."""
+    from adrt_pinv_gb300.device import Pipeline
+
+    def plan(n):
+        return pkg.Plan("hybrid", n, np.full(2 << n, 4.0), outer=(1.0, 2.0, 3))
+
+    assert all(Pipeline.ff_state_for(plan(n), "fp32") for n in (6, 7, 8, 9))
+    assert not any(Pipeline.ff_state_for(plan(n), "fp32") for n in (4, 5, 10, 11))
+    assert not Pipeline.ff_state_for(plan(8), "fp64")
+    assert not Pipeline.ff_state_for(plan(8), "fp32", "ff") and not Pipeline.ff_state_for(plan(8), "fp32", "fp64")
+
+
 @pytest.mark.parametrize("method,n", [("lp", 4), ("hybrid", 6), ("hybrid", 4), ("lp", 6)])
 def test_plan_matches_oracle(pkg, golden, method, n):
     name = {"lp": "lp", "hybrid": "hyb"}[method]
